@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""SpMM benchmark: algorithmic HBM GB/s of C = A*B on the power-law matrix.
+
+Workload (the configuration the headline metric is quoted on): A is
+1,000,000 x 1,000,000 CSR with row lengths Zipf(2.1) clipped to [1, 20000]
+and uniform columns (~4.6 M nonzeros), B is 1,000,000 x 64 FP32, seed 1;
+synthetic data from segscan_gb300.synth.  One step = one SpMM
+(C overwritten) through the C ABI.  Bytes per step are algorithmic:
+nnz*(4+4) + (M+1)*4 + U*N*4 + M*N*4 with U = distinct columns of A.  B and C
+(256 MB each) are larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's own CPU SpMM (its check path,
+test-cg/include/util/check.cuh:139-158, restated in oracle/oracle.c and run
+row-parallel on every host core) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SpMM HBM GB/s (algorithmic bytes), power-law 1e6x1e6 Zipf2.1 N=64 FP32"
+UNIT = "GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--N", type=int, default=64)
+    ap.add_argument("--strategy", default="auto")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(N: int):
+    from segscan_gb300 import synth
+    A = synth.powerlaw(1_000_000, 1_000_000, 2.1, 1, 20000, seed=1)
+    B = synth.dense(A.ncol, N, seed=2)
+    return A, B
+
+
+def config(A, N, extra=None):
+    cfg = {"workload": "spmm_powerlaw_1e6_zipf2.1_clip20000_n%d_fp32" % N, "nrow": A.nrow, "ncol": A.ncol,
+           "nnz": A.nnz, "N": N, "distinct_cols": A.distinct_columns(), "dtype_values": "f32",
+           "dtype_B": "f32", "dtype_C": "f32", "seed": 1,
+           "l2": "no flush: B and C (256 MB each) exceed the 126 MB L2"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel_file: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / kernel_file
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_full_workload:"):
+            try:
+                return int(float(line.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the GPU is under load."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.file, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        sm = []
+        smax = None
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for i, n in enumerate(names):
+                if r[5 + i].lower() == "active":
+                    reasons.add(n)
+        loaded = [x for x in sm if smax and x > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_spmm_time(A, B, threads: int, budget_s: float, min_iters: int = 2, max_iters: int = 50):
+    """Times the reference's CPU SpMM (oracle port) on A, B: seconds per pass."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_lib
+    times = []
+    start = time.perf_counter()
+    while len(times) < max_iters:
+        t0 = time.perf_counter()
+        oracle_lib.spmm_check_f32(A.indptr, A.indices, A.values, B, threads=threads)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= min_iters and time.perf_counter() - start > budget_s:
+            break
+    return statistics.median(times), len(times)
+
+
+def cpu_sample(A, B, target_s: float, threads: int):
+    """Row block of A whose CPU pass takes about target_s (the whole matrix if faster)."""
+    from segscan_gb300 import synth
+    t, _ = cpu_spmm_time(A, B, threads, 0.0, 1, 1)
+    if t <= target_s:
+        return A, "whole matrix", t
+    frac = target_s / t
+    rows = max(1, int(A.nrow * frac))
+    sub = synth.Csr(rows, A.ncol, A.indptr[:rows + 1].copy(), A.indices[:A.indptr[rows]].copy(),
+                    A.values[:A.indptr[rows]].copy())
+    return sub, f"first {rows} rows", None
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    from segscan_gb300 import synth
+    A, B = workload(args.N)
+    threads = os.cpu_count() or 1
+    sample, desc, _ = cpu_sample(A, B, 2.0, threads)
+    nbytes = synth.spmm_bytes(sample, args.N)
+    for _ in range(max(0, args.warmup)):
+        cpu_spmm_time(sample, B, threads, 0.0, 1, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle_lib
+        oracle_lib.spmm_check_f32(sample.indptr, sample.indices, sample.values, B, threads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    gbs = nbytes / dt / 1e9
+    line = {"metric": METRIC, "value": gbs, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(A, args.N, {"sample": desc}), "impl": "reference",
+            "cpu_baseline": {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{desc} of the workload, row-parallel restatement of "
+                                       "spmm_reference_host (check.cuh:139-158)"},
+            "e2e": {"value": gbs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def choose(args, A_dev, N):
+    from segscan_gb300 import api, autotune
+    if args.strategy != "auto":
+        return args.strategy, api.default_knobs(args.strategy, N)
+    return autotune.best(A_dev, N)
+
+
+def run_ours(args):
+    import torch
+    from segscan_gb300 import api, synth
+
+    ws_, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws_ > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    A, B = workload(args.N)
+    N = args.N
+    nbytes = synth.spmm_bytes(A, N)
+    Ad = api.CsrMatrix.from_host(A, dev)
+    Bd = torch.from_numpy(B).to(dev)
+    strategy, knobs = choose(args, Ad, N)
+    C = torch.empty((A.nrow, N), dtype=torch.float32, device=dev)
+    wsz = api.spmm_workspace_size(Ad, N, strategy, knobs)
+    work = torch.empty(wsz + 256, dtype=torch.uint8, device=dev) if wsz else None
+    stream = torch.cuda.current_stream(dev)
+    kernels_per_step = 2 if strategy in ("ebsr", "ebpr") else 1
+
+    def step():
+        api.spmm(Ad, Bd, strategy, knobs=knobs, out=C, workspace=work, stream=stream)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+
+    def barrier():
+        if ws_ > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    barrier()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    t = e0.elapsed_time(e1) / 1e3 / args.steps
+    if ws_ > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+
+    # end to end through the public API: host inputs in pinned memory,
+    # H2D of A and B, the SpMM, D2H of C, every step
+    h_indptr = torch.from_numpy(A.indptr).pin_memory()
+    h_indices = torch.from_numpy(A.indices).pin_memory()
+    h_values = torch.from_numpy(A.values).pin_memory()
+    h_B = torch.from_numpy(B).pin_memory()
+    h_C = torch.empty((A.nrow, N), dtype=torch.float32).pin_memory()
+    d_indptr = torch.empty_like(Ad.indptr)
+    d_indices = torch.empty_like(Ad.indices)
+    d_values = torch.empty_like(Ad.values)
+    d_B = torch.empty_like(Bd)
+    Ae = api.CsrMatrix(A.nrow, A.ncol, d_indptr, d_indices, d_values)
+    h2d = sum(x.numel() * x.element_size() for x in (h_indptr, h_indices, h_values, h_B))
+    d2h = h_C.numel() * h_C.element_size()
+
+    def e2e_step():
+        d_indptr.copy_(h_indptr, non_blocking=True)
+        d_indices.copy_(h_indices, non_blocking=True)
+        d_values.copy_(h_values, non_blocking=True)
+        d_B.copy_(h_B, non_blocking=True)
+        api.spmm(Ae, d_B, strategy, knobs=knobs, out=C, workspace=work, stream=stream)
+        h_C.copy_(C, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    t_e2e = e0.elapsed_time(e1) / 1e3 / args.e2e_steps
+    if ws_ > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    clocks = sampler.stop()
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    achieved = nbytes / t / 1e9
+    kernel_file = f"spmm_{strategy}_powerlaw_n{N}.md"
+    line = {
+        "metric": METRIC, "value": achieved * ws_, "unit": UNIT, "n_gpus": ws_, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config(A, N, {"strategy": strategy, "knobs": knobs.as_dict(), "parallelism": f"replica x{ws_}"}),
+        "gflops": 2.0 * A.nnz * N / t / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic_from_profiles(kernel_file),
+                     "kernel": f"{strategy} SpMM step (main kernel + carry fix-up)",
+                     "bytes_per_launch": nbytes},
+        "e2e": {"value": nbytes / t_e2e / 1e9 * ws_, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": kernels_per_step * args.steps,
+        "clocks": clocks,
+    }
+    if ws_ == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample, desc, _ = cpu_sample(A, B, 2.0, threads)
+        sec, iters = cpu_spmm_time(sample, B, threads, 10.0)
+        line["cpu_baseline"] = {"value": synth.spmm_bytes(sample, N) / sec / 1e9, "unit": UNIT, "cores": threads,
+                                "kind": "port", "sample": f"{desc}, {iters} passes, row-parallel restatement of "
+                                                          "spmm_reference_host (check.cuh:139-158)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,242 @@
+/*
+ * segscan_gb300 - C ABI of the GB300 (sm_103a) SpMM / segment_coo library.
+ *
+ * The reference (zhang677/segScan) has no library boundary: its operator API
+ * is header-only C++ templates that a driver instantiates per knob tuple.
+ * This header is the drop-in replacement for those templates: the same four
+ * SpMM strategies and the segment_coo family, with the same tuning knobs
+ * passed at run time instead of as template arguments.  Every entry point
+ * cites the reference interface it replaces.  include/segscan_gb300.hpp
+ * re-creates the reference's template signatures on top of this ABI.
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers owned by the caller.  Nothing
+ *    here allocates device memory; scratch space comes from the caller
+ *    through (ws, ws_bytes), sized by the matching *_workspace_size query.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream).  Every call is stream-ordered and asynchronous; calls that
+ *    share no buffers may run concurrently on different streams.
+ *  - Errors come back as ss_status.  Nothing calls exit().  Argument and
+ *    knob errors are detected on the host before any launch.  Malformed
+ *    device data (column out of range, indptr not monotone, unsorted
+ *    segment index) never makes a kernel access memory out of bounds; the
+ *    ss_*_validate calls report it.
+ *  - Outputs: with accumulate = 0 the output is overwritten (C = A*B), every
+ *    row including empty rows is written, and the caller need not zero it.
+ *    With accumulate = 1 the result is added (C += A*B), matching the
+ *    reference launchers whose callers pre-zero C.
+ *  - Values and B share one storage type (SS_F32, SS_BF16 or SS_F16);
+ *    arithmetic is FP32 in every kernel; C is FP32 or the storage type.
+ */
+#ifndef SEGSCAN_GB300_H
+#define SEGSCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SS_VERSION_MAJOR 0
+#define SS_VERSION_MINOR 1
+
+typedef enum {
+  SS_OK = 0,
+  SS_ERR_INVALID_ARG = 1,       /* null pointer, negative size, bad enum */
+  SS_ERR_UNSUPPORTED_KNOBS = 2, /* knob tuple outside the compiled table */
+  SS_ERR_WORKSPACE = 3,         /* ws too small or misaligned */
+  SS_ERR_CUDA = 4,              /* a CUDA runtime call failed */
+  SS_ERR_ALIGNMENT = 5,         /* a pointer is not aligned to its element */
+  SS_ERR_BAD_DATA = 6,          /* reported by the *_validate calls */
+  SS_ERR_TIMEOUT = 7,           /* a bounded device wait gave up */
+  SS_ERR_CAPACITY = 8           /* size beyond a fixed capacity */
+} ss_status;
+
+typedef enum { SS_F32 = 0, SS_BF16 = 1, SS_F16 = 2 } ss_dtype;
+
+typedef enum {
+  SS_EBPR = 0, /* element-balanced, parallel reduction  */
+  SS_RBPR = 1, /* row-balanced, parallel reduction      */
+  SS_EBSR = 2, /* element-balanced, sequential reduction */
+  SS_RBSR = 3  /* row-balanced, sequential reduction    */
+} ss_strategy;
+
+typedef enum { SS_SUM = 0, SS_MAX = 1, SS_MEAN = 2 } ss_reduce;
+
+typedef enum {
+  SS_SEG_PR = 0, /* shuffle-scan family: segment_coo, segment_coo_new            */
+  SS_SEG_SR = 1  /* sequential family: segment_coo_sr, _noshmem_sr,
+                    _noshmem_lessatom_sr, _sorted_sr                               */
+} ss_seg_strategy;
+
+/* CSR matrix A [nrow x ncol] (SpMatCsrDescr_t, test-cg/include/dataloader/
+ * dataloader.hpp:146-168).  values == NULL means every stored value is 1
+ * (__guard_load_default_one, test-cg/include/util/check.cuh:104-111). */
+typedef struct {
+  int32_t nrow, ncol, nnz;
+  const int32_t *indptr;  /* [nrow + 1], indptr[0] = 0, indptr[nrow] = nnz */
+  const int32_t *indices; /* [nnz], column of each nonzero, in [0, ncol)   */
+  const void *values;     /* [nnz] of value_dtype, or NULL                 */
+  int32_t value_dtype;    /* ss_dtype                                       */
+} ss_csr;
+
+/* Tuning knobs, the reference's template parameters at run time.
+ *   group_factor     group_size = 1 << group_factor lanes that reduce together
+ *                    (ebpr, rbpr) or that share one staged nonzero tile (ebsr)
+ *   tile_factor      tile_size  = 1 << tile_factor (the README's tail_factor):
+ *                    lanes per row (rbpr), nonzeros per step (ebpr), column
+ *                    tile width (ebpr, rbpr, rbsr)
+ *   thread_per_block threads per CTA
+ *   block_numer/block_denom  block_factor: workers = nrow * numer / denom
+ *   coarsen_factor   elements of N per lane (ebsr CoarsenFactor, rbsr
+ *                    coarsen_factor; ebpr/rbpr derive it from N as the
+ *                    reference does)
+ *   thread_nz        staged tiles per worker step (ebsr ThreadNz)
+ *   kahan_threshold  rows (segments) longer than this accumulate with
+ *                    compensated summation; <= 0 selects the default
+ *                    (1024), INT32_MAX disables it. */
+typedef struct {
+  int32_t group_factor;
+  int32_t tile_factor;
+  int32_t thread_per_block;
+  int32_t block_numer;
+  int32_t block_denom;
+  int32_t coarsen_factor;
+  int32_t thread_nz;
+  int32_t kahan_threshold;
+} ss_knobs;
+
+/* ---------------------------------------------------------------- */
+/* Library                                                            */
+/* ---------------------------------------------------------------- */
+int ss_version(void);                      /* major * 100 + minor */
+const char *ss_status_string(int status);  /* static string */
+/* Text of the last failure on the calling host thread ("" if none). */
+const char *ss_last_error(void);
+/* Knob tuple the reference's README reports as best static choice for a
+ * strategy (test-cg README.md:168-210), used when knobs == NULL. */
+ss_status ss_default_knobs(int strategy, int N, ss_knobs *out);
+
+/* ---------------------------------------------------------------- */
+/* SpMM: C[nrow x N] (=|+=) A[nrow x ncol] * B[ncol x N], row-major.  */
+/* ---------------------------------------------------------------- */
+
+/* Scratch bytes a strategy needs for (A, N, knobs); 0 for rbpr/rbsr. */
+ss_status ss_spmm_workspace_size(int strategy, const ss_csr *A, int N,
+                                 const ss_knobs *knobs, size_t *bytes);
+
+/* Replaces csrspmm_parreduce_nnzbalance_cg<Index, DType, group_factor,
+ * thread_per_block, tile_factor, block_numer, block_denom>
+ * (test-cg/include/spmm/spmm_cg.cuh:176-178). */
+ss_status ss_spmm_ebpr(const ss_csr *A, int N, const void *B, void *C,
+                       int c_dtype, int accumulate, const ss_knobs *knobs,
+                       void *ws, size_t ws_bytes, void *stream);
+
+/* Replaces csrspmm_parreduce_rowbalance_cg<...same knobs...>
+ * (spmm_cg.cuh:333-335). */
+ss_status ss_spmm_rbpr(const ss_csr *A, int N, const void *B, void *C,
+                       int c_dtype, int accumulate, const ss_knobs *knobs,
+                       void *ws, size_t ws_bytes, void *stream);
+
+/* Replaces csrspmm_rowcaching_nnzbalance_cg<Index, DType, group_factor,
+ * thread_per_block, CoarsenFactor, ThreadNz, block_numer, block_denom>
+ * (spmm_cg.cuh:553-555). */
+ss_status ss_spmm_ebsr(const ss_csr *A, int N, const void *B, void *C,
+                       int c_dtype, int accumulate, const ss_knobs *knobs,
+                       void *ws, size_t ws_bytes, void *stream);
+
+/* Replaces csrspmm_seqreduce_rowbalance_cg<Index, DType, coarsen_factor,
+ * thread_per_block, tile_factor, block_numer, block_denom>
+ * (spmm_cg.cuh:664-666). */
+ss_status ss_spmm_rbsr(const ss_csr *A, int N, const void *B, void *C,
+                       int c_dtype, int accumulate, const ss_knobs *knobs,
+                       void *ws, size_t ws_bytes, void *stream);
+
+/* One entry for any strategy (the four calls above dispatch here). */
+ss_status ss_spmm(int strategy, const ss_csr *A, int N, const void *B,
+                  void *C, int c_dtype, int accumulate, const ss_knobs *knobs,
+                  void *ws, size_t ws_bytes, void *stream);
+
+/* ---------------------------------------------------------------- */
+/* segment_coo: dst[index[i], :] (op)= src[i, :] over sorted index.    */
+/* ---------------------------------------------------------------- */
+
+ss_status ss_segment_coo_workspace_size(int seg_strategy, int nnz, int N,
+                                        const ss_knobs *knobs, size_t *bytes);
+
+/* Replaces segment_coo / segment_coo_new (SS_SEG_PR) and segment_coo_sr,
+ * segment_coo_noshmem_sr, segment_coo_noshmem_lessatom_sr,
+ * segment_coo_sorted_sr (SS_SEG_SR)
+ * (new-cg/include/segscan/segscan.cuh:150-151, 327-328, 817-818, 868-869,
+ * 918-919, 974-975), which compute the sum only; max and mean are added.
+ * src [nnz x N] of src_dtype, index [nnz] sorted ascending, dst
+ * [dst_len x N] FP32.  Empty segments get 0.  accumulate = 1 is allowed for
+ * SS_SUM only (the reference's dst += contract). */
+ss_status ss_segment_coo(int seg_strategy, const void *src, int src_dtype,
+                         const int32_t *index, int nnz, int N, int dst_len,
+                         float *dst, int reduce, int accumulate,
+                         const ss_knobs *knobs, void *ws, size_t ws_bytes,
+                         void *stream);
+
+/* ---------------------------------------------------------------- */
+/* Row assignment, transpose, SDDMM, validation                        */
+/* ---------------------------------------------------------------- */
+
+/* rows[i] = row owning nonzero elems[i]: upper_bound(indptr[1..M-1], e) - 1,
+ * empty rows skipped, e >= nnz gives M-1.  Replaces
+ * binary_search_segment_number (test-cg/include/util/check.cuh:88-102). When
+ * elems == NULL, rows[e] is written for every e in [0, count). */
+ss_status ss_row_ids(const int32_t *indptr, int M, int nnz,
+                     const int32_t *elems, int64_t count, int32_t *rows,
+                     void *stream);
+
+/* Transposed pattern of A: t_indptr [ncol + 1], t_indices [nnz] (row ids),
+ * perm [nnz] (source nonzero of each transposed entry).  Stable: within a
+ * column the entries keep A's CSR order, so the result is bit-identical to
+ * the host counting sort transpose + compressedRow
+ * (test-cg/include/dataloader/dataloader.hpp:109-144). */
+ss_status ss_csr_transpose_workspace_size(const ss_csr *A, size_t *bytes);
+ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr,
+                           int32_t *t_indices, int32_t *perm, void *ws,
+                           size_t ws_bytes, void *stream);
+
+/* out[p] = perm-gathered values: out[q] = values[perm[q]] (any dtype). */
+ss_status ss_gather_values(const void *values, int dtype, const int32_t *perm,
+                           int nnz, void *out, void *stream);
+
+/* SDDMM for the backward of C = A*B: dvals[p] = dot(dC[i, :], B[k, :]) for
+ * every stored nonzero p = (i, k).  dC is FP32 [nrow x N]; B is A's value
+ * dtype [ncol x N]; dvals is FP32 [nnz].  No counterpart in the reference. */
+ss_status ss_sddmm(const ss_csr *A, int N, const float *dC, const void *B,
+                   float *dvals, void *stream);
+
+/* Checks indptr (0 first, nnz last, monotone) and column range; writes 0 to
+ * *d_flag (device int) when A is well formed, else a nonzero code. */
+ss_status ss_csr_validate(const ss_csr *A, int32_t *d_flag, void *stream);
+/* Checks index sorted and inside [0, dst_len); same flag convention. */
+ss_status ss_index_validate(const int32_t *index, int nnz, int dst_len,
+                            int32_t *d_flag, void *stream);
+
+/* ---------------------------------------------------------------- */
+/* Batched SpMM: many independent CSR matrices in one persistent launch */
+/* ---------------------------------------------------------------- */
+
+/* A batch plan lives in caller memory: a device table built by
+ * ss_batch_plan from host descriptors.  mats/B/C are host arrays of
+ * `count` entries holding device pointers.  Per-matrix knobs (may be NULL)
+ * choose the row-team shape of each matrix.  Not in the reference. */
+ss_status ss_batch_plan_size(int count, const ss_csr *mats, int N,
+                             size_t *host_bytes, size_t *dev_bytes);
+ss_status ss_batch_plan(int count, const ss_csr *mats, int N,
+                        const void *const *B, void *const *C, int c_dtype,
+                        const ss_knobs *per_mat, void *host_buf,
+                        size_t host_bytes, void *dev_buf, size_t dev_bytes,
+                        void *stream);
+ss_status ss_spmm_batched(const void *dev_buf, size_t dev_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEGSCAN_GB300_H */

@@ -1,0 +1,310 @@
+"""Host API over the C ABI, for Python callers holding torch CUDA tensors.
+
+The reference's operator API is a set of C++ launcher templates
+(test-cg/include/spmm/spmm_cg.cuh:176-178, 333-335, 553-555, 664-666;
+new-cg/include/segscan/segscan.cuh:150-151, 327-328, 817-818, 868-869,
+918-919, 974-975).  The functions named after them here take the same
+arguments in the same order (the template knobs become keyword arguments)
+and keep their output contract: the three atomic-based strategies and the
+segment_coo family ADD into a caller-zeroed output, rbsr overwrites.  The
+generic ``spmm`` / ``segment`` calls overwrite by default.
+
+torch supplies device memory and the current stream only; every computation
+is a call into libsegscan_gb300.so.  Nothing here falls back to PyTorch.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import Dtype, Reduce, SegStrategy, SsCsr, SsKnobs, Strategy
+
+_TORCH_DTYPE = {Dtype.F32: torch.float32, Dtype.BF16: torch.bfloat16, Dtype.F16: torch.float16}
+_DTYPE_OF = {v: k for k, v in _TORCH_DTYPE.items()}
+
+STRATEGIES = {"ebpr": Strategy.EBPR, "rbpr": Strategy.RBPR, "ebsr": Strategy.EBSR, "rbsr": Strategy.RBSR}
+SEG_STRATEGIES = {"pr": SegStrategy.PR, "sr": SegStrategy.SR}
+REDUCES = {"sum": Reduce.SUM, "max": Reduce.MAX, "mean": Reduce.MEAN}
+
+
+def dtype_code(t: torch.dtype) -> Dtype:
+    try:
+        return _DTYPE_OF[t]
+    except KeyError:
+        raise TypeError(f"unsupported dtype {t}; use float32, bfloat16 or float16") from None
+
+
+def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+def _need_cuda(name: str, t: torch.Tensor, dtype: Optional[torch.dtype] = None) -> None:
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+
+
+@dataclasses.dataclass
+class CsrMatrix:
+    """Device CSR matrix (the reference's SpMatCsrDescr_t, test-cg/include/
+    dataloader/dataloader.hpp:146-168).  values=None means all ones."""
+
+    nrow: int
+    ncol: int
+    indptr: torch.Tensor
+    indices: torch.Tensor
+    values: Optional[torch.Tensor]
+
+    @property
+    def nnz(self) -> int:
+        return int(self.indices.numel())
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return self.values.dtype if self.values is not None else torch.float32
+
+    @classmethod
+    def from_host(cls, csr, device="cuda", dtype: torch.dtype = torch.float32, values: bool = True):
+        ip = torch.from_numpy(np.ascontiguousarray(csr.indptr, dtype=np.int32)).to(device)
+        ix = torch.from_numpy(np.ascontiguousarray(csr.indices, dtype=np.int32)).to(device)
+        v = None
+        if values:
+            v = torch.from_numpy(np.ascontiguousarray(csr.values, dtype=np.float32)).to(device).to(dtype)
+        return cls(int(csr.nrow), int(csr.ncol), ip, ix, v)
+
+    def with_values(self, values: Optional[torch.Tensor]) -> "CsrMatrix":
+        return CsrMatrix(self.nrow, self.ncol, self.indptr, self.indices, values)
+
+    def descr(self) -> SsCsr:
+        _need_cuda("indptr", self.indptr, torch.int32)
+        _need_cuda("indices", self.indices, torch.int32)
+        if self.values is not None:
+            _need_cuda("values", self.values)
+        return SsCsr(self.nrow, self.ncol, self.nnz, _ptr(self.indptr), _ptr(self.indices),
+                     _ptr(self.values), int(dtype_code(self.dtype)))
+
+
+def default_knobs(strategy: str, N: int = 64) -> SsKnobs:
+    k = SsKnobs()
+    _lib.call("ss_default_knobs", int(STRATEGIES[strategy]), N, ctypes.byref(k))
+    return k
+
+
+def make_knobs(strategy: str, N: int = 64, **kw) -> SsKnobs:
+    """Default knobs of a strategy with the given fields replaced."""
+    k = default_knobs(strategy, N)
+    for name, val in kw.items():
+        if val is None:
+            continue
+        if not hasattr(k, name):
+            raise TypeError(f"unknown knob {name}")
+        setattr(k, name, int(val))
+    return k
+
+
+def _workspace(nbytes: int, device) -> Optional[torch.Tensor]:
+    if nbytes == 0:
+        return None
+    return torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+
+
+def _aligned(ws: Optional[torch.Tensor]) -> tuple[Optional[int], int]:
+    if ws is None:
+        return None, 0
+    p = ws.data_ptr()
+    off = (-p) % 256
+    return p + off, ws.numel() - off
+
+
+def spmm_workspace_size(A: CsrMatrix, N: int, strategy: str, knobs: Optional[SsKnobs] = None) -> int:
+    n = ctypes.c_size_t()
+    d = A.descr()
+    _lib.call("ss_spmm_workspace_size", int(STRATEGIES[strategy]), ctypes.byref(d), N,
+              ctypes.byref(knobs) if knobs is not None else None, ctypes.byref(n))
+    return int(n.value)
+
+
+def spmm(A: CsrMatrix, B: torch.Tensor, strategy: str = "ebsr", knobs: Optional[SsKnobs] = None,
+         out: Optional[torch.Tensor] = None, accumulate: bool = False,
+         out_dtype: Optional[torch.dtype] = None, workspace: Optional[torch.Tensor] = None,
+         stream=None) -> torch.Tensor:
+    """C = A @ B (or C += A @ B with accumulate=True) with one of the four strategies."""
+    if B.dim() != 2 or B.shape[0] != A.ncol:
+        raise ValueError(f"B must be [{A.ncol}, N], got {tuple(B.shape)}")
+    _need_cuda("B", B, A.dtype)
+    N = int(B.shape[1])
+    cdt = out_dtype or (out.dtype if out is not None else torch.float32)
+    if out is None:
+        out = torch.empty((A.nrow, N), dtype=cdt, device=B.device)
+    _need_cuda("out", out, cdt)
+    if tuple(out.shape) != (A.nrow, N):
+        raise ValueError(f"out must be [{A.nrow}, {N}]")
+    d = A.descr()
+    kp = ctypes.byref(knobs) if knobs is not None else None
+    if workspace is None:
+        workspace = _workspace(spmm_workspace_size(A, N, strategy, knobs), B.device)
+    wp, wn = _aligned(workspace)
+    _lib.call("ss_spmm", int(STRATEGIES[strategy]), ctypes.byref(d), N, _ptr(B), _ptr(out),
+              int(dtype_code(cdt)), int(bool(accumulate)), kp, wp, wn, _stream(stream))
+    return out
+
+
+def segment_workspace_size(nnz: int, N: int, strategy: str = "sr", knobs: Optional[SsKnobs] = None) -> int:
+    n = ctypes.c_size_t()
+    _lib.call("ss_segment_coo_workspace_size", int(SEG_STRATEGIES[strategy]), nnz, N,
+              ctypes.byref(knobs) if knobs is not None else None, ctypes.byref(n))
+    return int(n.value)
+
+
+def segment(src: torch.Tensor, index: torch.Tensor, dst_len: int, reduce: str = "sum",
+            strategy: str = "sr", knobs: Optional[SsKnobs] = None, out: Optional[torch.Tensor] = None,
+            accumulate: bool = False, stream=None) -> torch.Tensor:
+    """dst[index[i], :] (op)= src[i, :] over a sorted index; op in sum / max / mean."""
+    if src.dim() != 2 or index.dim() != 1 or index.shape[0] != src.shape[0]:
+        raise ValueError("src must be [nnz, N] and index [nnz]")
+    _need_cuda("src", src)
+    _need_cuda("index", index, torch.int32)
+    nnz, N = int(src.shape[0]), int(src.shape[1])
+    if out is None:
+        out = torch.empty((dst_len, N), dtype=torch.float32, device=src.device)
+    _need_cuda("out", out, torch.float32)
+    ws = _workspace(segment_workspace_size(nnz, N, strategy, knobs), src.device)
+    wp, wn = _aligned(ws)
+    _lib.call("ss_segment_coo", int(SEG_STRATEGIES[strategy]), _ptr(src), int(dtype_code(src.dtype)),
+              _ptr(index), nnz, N, int(dst_len), _ptr(out), int(REDUCES[reduce]), int(bool(accumulate)),
+              ctypes.byref(knobs) if knobs is not None else None, wp, wn, _stream(stream))
+    return out
+
+
+def row_ids(indptr: torch.Tensor, nnz: int, elems: Optional[torch.Tensor] = None, stream=None) -> torch.Tensor:
+    """Row of each nonzero (binary_search_segment_number, check.cuh:88-102)."""
+    _need_cuda("indptr", indptr, torch.int32)
+    M = int(indptr.numel()) - 1
+    count = nnz if elems is None else int(elems.numel())
+    rows = torch.empty(count, dtype=torch.int32, device=indptr.device)
+    if elems is not None:
+        _need_cuda("elems", elems, torch.int32)
+    _lib.call("ss_row_ids", _ptr(indptr), M, nnz, _ptr(elems), count, _ptr(rows), _stream(stream))
+    return rows
+
+
+def validate(A: CsrMatrix, stream=None) -> int:
+    """0 when A is well formed, else the flag bits of ss_csr_validate (synchronises)."""
+    flag = torch.zeros(1, dtype=torch.int32, device=A.indptr.device)
+    d = A.descr()
+    _lib.call("ss_csr_validate", ctypes.byref(d), _ptr(flag), _stream(stream))
+    return int(flag.item())
+
+
+def validate_index(index: torch.Tensor, dst_len: int, stream=None) -> int:
+    flag = torch.zeros(1, dtype=torch.int32, device=index.device)
+    _lib.call("ss_index_validate", _ptr(index), int(index.numel()), int(dst_len), _ptr(flag), _stream(stream))
+    return int(flag.item())
+
+
+# ---------------------------------------------------------------------------
+# Reference-named operators (same argument order; knobs as keywords)
+# ---------------------------------------------------------------------------
+def _ref_spmm(strategy: str, A: CsrMatrix, N: int, B: torch.Tensor, C: torch.Tensor, accumulate: int,
+              **kw) -> None:
+    if B.shape[1] != N or C.shape[1] != N:
+        raise ValueError("N does not match B / C")
+    spmm(A, B, strategy, knobs=make_knobs(strategy, N, **kw), out=C, accumulate=bool(accumulate))
+
+
+def csrspmm_parreduce_nnzbalance_cg(A, N, B, C, *, group_factor, thread_per_block, tile_factor,
+                                    block_numer, block_denom):
+    """ebpr: C += A*B (spmm_cg.cuh:176-178)."""
+    _ref_spmm("ebpr", A, N, B, C, 1, group_factor=group_factor, thread_per_block=thread_per_block,
+              tile_factor=tile_factor, block_numer=block_numer, block_denom=block_denom)
+
+
+def csrspmm_parreduce_rowbalance_cg(A, N, B, C, *, group_factor, thread_per_block, tile_factor,
+                                    block_numer, block_denom):
+    """rbpr: C += A*B (spmm_cg.cuh:333-335)."""
+    _ref_spmm("rbpr", A, N, B, C, 1, group_factor=group_factor, thread_per_block=thread_per_block,
+              tile_factor=tile_factor, block_numer=block_numer, block_denom=block_denom)
+
+
+def csrspmm_rowcaching_nnzbalance_cg(A, N, B, C, *, group_factor, thread_per_block, CoarsenFactor,
+                                     ThreadNz, block_numer, block_denom):
+    """ebsr: C += A*B (spmm_cg.cuh:553-555)."""
+    _ref_spmm("ebsr", A, N, B, C, 1, group_factor=group_factor, thread_per_block=thread_per_block,
+              coarsen_factor=CoarsenFactor, thread_nz=ThreadNz, block_numer=block_numer,
+              block_denom=block_denom)
+
+
+def csrspmm_seqreduce_rowbalance_cg(A, N, B, C, *, coarsen_factor, thread_per_block, tile_factor,
+                                    block_numer, block_denom):
+    """rbsr: C = A*B (spmm_cg.cuh:664-666)."""
+    _ref_spmm("rbsr", A, N, B, C, 0, coarsen_factor=coarsen_factor, thread_per_block=thread_per_block,
+              tile_factor=tile_factor, block_numer=block_numer, block_denom=block_denom)
+
+
+def _seg_knobs(strategy: str, **kw) -> SsKnobs:
+    k = SsKnobs()
+    base = dict(group_factor=5 if strategy == "pr" else 4, tile_factor=5, thread_per_block=256,
+                block_numer=1, block_denom=1, coarsen_factor=4, thread_nz=8, kahan_threshold=1024)
+    base.update({k_: v for k_, v in kw.items() if v is not None})
+    for name, val in base.items():
+        setattr(k, name, int(val))
+    return k
+
+
+def _ref_segment(strategy, src, index, nnz, N, dst, **kw) -> None:
+    if src.shape != (nnz, N) or dst.shape[1] != N:
+        raise ValueError("shape mismatch")
+    segment(src, index, int(dst.shape[0]), "sum", strategy, knobs=_seg_knobs(strategy, **kw), out=dst,
+            accumulate=True)
+
+
+def segment_coo(src, index, nnz, N, dst, *, group_factor, thread_per_block, tile_factor, block_numer,
+                block_denom):
+    """segscan.cuh:150-151: dst[index[i]] += src[i] (shuffle-scan family)."""
+    _ref_segment("pr", src, index, nnz, N, dst, group_factor=group_factor, thread_per_block=thread_per_block,
+                 tile_factor=tile_factor, block_numer=block_numer, block_denom=block_denom)
+
+
+def segment_coo_new(src, index, nnz, N, dst, *, group_factor, thread_per_block, tile_factor, blockDimY):
+    """segscan.cuh:327-328.  The reference's 2-D (nnz x column) split maps to
+    the shuffle-scan family with one nonzero step per worker."""
+    _ref_segment("pr", src, index, nnz, N, dst, group_factor=group_factor, thread_per_block=thread_per_block,
+                 tile_factor=tile_factor, block_numer=1, block_denom=max(1, 1 << tile_factor))
+
+
+def segment_coo_sr(src, index, nnz, N, dst, *, group_factor, thread_per_block, CoarsenFactor, ThreadNz,
+                   block_numer, block_denom):
+    """segscan.cuh:817-818 (smem-staged sequential)."""
+    _ref_segment("sr", src, index, nnz, N, dst, group_factor=group_factor, thread_per_block=thread_per_block,
+                 coarsen_factor=CoarsenFactor, thread_nz=ThreadNz, block_numer=block_numer,
+                 block_denom=block_denom)
+
+
+segment_coo_noshmem_sr = segment_coo_sr            # segscan.cuh:868-869
+segment_coo_noshmem_lessatom_sr = segment_coo_sr   # segscan.cuh:918-919
+
+
+def segment_coo_sorted_sr(src, index, nnz, N, dst, *, CoarsenFactor, ThreadNz, DtileSize, DtileNum, BlockDimY):
+    """segscan.cuh:974-975: a worker of DtileSize lanes along N reduces a run
+    of ThreadNz consecutive elements; DtileNum x BlockDimY workers per block."""
+    gf = max(0, min(5, int(DtileSize).bit_length() - 1))
+    G = 1 << gf
+    tpb = max(G, min(1024, G * int(DtileNum) * int(BlockDimY)))
+    tpb -= tpb % G
+    _ref_segment("sr", src, index, nnz, N, dst, group_factor=gf, thread_per_block=tpb,
+                 coarsen_factor=CoarsenFactor, thread_nz=max(1, int(ThreadNz) // G),
+                 block_numer=1, block_denom=1)

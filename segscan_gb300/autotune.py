@@ -1,0 +1,154 @@
+"""Autotuner: picks the SpMM strategy and knob tuple for a matrix.
+
+The reference tunes by hand: a driver instantiates every knob tuple of a
+grid (test-cg/src/test.cu:58-330, grids in test-cg/src/params.md) and an
+Nsight Compute sweep ranks them offline (test-cg/src/test.py:49-59,
+count.py).  Here the candidates (the README's best static tuples,
+README.md:168-210, and params.md-style grids, plus the chunk sizes this
+implementation favours) are timed once on the device with CUDA events and the
+winner is cached by a shape signature built from row-length statistics, so
+matrices of the same shape class reuse it without measuring again.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import threading
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import api
+from ._lib import SsKnobs
+
+_LOCK = threading.Lock()
+_MEM: dict = {}
+
+
+def cache_path() -> Path:
+    p = os.environ.get("SEGSCAN_TUNE_CACHE")
+    if p:
+        return Path(p)
+    return Path(os.path.expanduser("~")) / ".cache" / "segscan_gb300" / "tune.json"
+
+
+def features(A: api.CsrMatrix) -> dict:
+    lengths = torch.diff(A.indptr).to(torch.float64)
+    M = max(1, A.nrow)
+    mean = float(lengths.mean()) if A.nrow else 0.0
+    std = float(lengths.std()) if A.nrow > 1 else 0.0
+    return {"M": A.nrow, "K": A.ncol, "nnz": A.nnz, "mean": mean, "cv": std / mean if mean > 0 else 0.0,
+            "max": int(lengths.max()) if A.nrow else 0,
+            "frac_long": float((lengths > 32).sum()) / M}
+
+
+def signature(A: api.CsrMatrix, N: int, f: Optional[dict] = None) -> str:
+    f = f or features(A)
+    lg = lambda x: int(round(math.log2(max(1, x))))
+    cvb = 0 if f["cv"] < 0.5 else 1 if f["cv"] < 2 else 2 if f["cv"] < 8 else 3
+    return f"M{lg(f['M'])}_nnz{lg(f['nnz'])}_mean{lg(f['mean'] + 1)}_max{lg(f['max'] + 1)}_cv{cvb}_N{N}_{A.dtype}"
+
+
+def candidates(N: int) -> list[tuple[str, dict]]:
+    """Strategy / knob candidates (README best static tuples, params.md grids,
+    and longer ebsr chunks, which suit the carry design)."""
+    c: list[tuple[str, dict]] = []
+    for gf, denom in ((5, 8), (5, 16), (4, 4)):
+        c.append(("ebpr", dict(group_factor=gf, tile_factor=5, block_denom=denom)))
+    for gf, tf, denom in ((3, 3, 2), (2, 2, 1), (4, 4, 2)):
+        c.append(("rbpr", dict(group_factor=gf, tile_factor=tf, block_denom=denom)))
+    lanes_gf = max(0, min(5, int(math.log2(max(1, N // 4)))))
+    for gf in sorted({lanes_gf, max(0, lanes_gf - 1)}):
+        for tnz in (2, 4, 8, 16, 32):
+            c.append(("ebsr", dict(group_factor=gf, coarsen_factor=4, thread_nz=tnz, block_denom=1)))
+    for cf, tf in ((4, 5), (4, 6), (2, 5)):
+        c.append(("rbsr", dict(coarsen_factor=cf, tile_factor=tf)))
+    return c
+
+
+def heuristic(f: dict, N: int) -> tuple[str, dict]:
+    """Choice without measuring: element-balanced sequential for skewed rows,
+    row-balanced sequential for short regular rows."""
+    lanes_gf = max(0, min(5, int(math.log2(max(1, N // 4)))))
+    if f["cv"] > 1.0 or f["max"] > 256:
+        return "ebsr", dict(group_factor=lanes_gf, coarsen_factor=4, thread_nz=8, block_denom=1)
+    return "rbsr", dict(coarsen_factor=4, tile_factor=max(0, min(7, int(math.log2(max(1, N))))))
+
+
+def _load_disk() -> dict:
+    p = cache_path()
+    try:
+        return json.loads(p.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_disk(key: str, val: dict) -> None:
+    p = cache_path()
+    try:
+        p.parent.mkdir(parents=True, exist_ok=True)
+        d = _load_disk()
+        d[key] = val
+        tmp = p.with_suffix(".tmp")
+        tmp.write_text(json.dumps(d, indent=1, sort_keys=True))
+        os.replace(tmp, p)
+    except OSError:
+        pass
+
+
+def time_candidate(A: api.CsrMatrix, B: torch.Tensor, strategy: str, knobs: SsKnobs, iters: int = 5) -> float:
+    out = torch.empty((A.nrow, B.shape[1]), dtype=torch.float32, device=B.device)
+    ws_bytes = api.spmm_workspace_size(A, B.shape[1], strategy, knobs)
+    ws = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=B.device) if ws_bytes else None
+    api.spmm(A, B, strategy, knobs=knobs, out=out, workspace=ws)
+    s = torch.cuda.current_stream(B.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(iters):
+        api.spmm(A, B, strategy, knobs=knobs, out=out, workspace=ws)
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / iters
+
+
+def tune(A: api.CsrMatrix, N: int, B: Optional[torch.Tensor] = None, iters: int = 5) -> list[tuple[float, str, dict]]:
+    """Times every candidate; returns [(ms, strategy, knob dict)] sorted."""
+    if B is None:
+        B = torch.rand((A.ncol, N), device=A.indptr.device, dtype=torch.float32).to(A.dtype)
+    res = []
+    for strategy, kw in candidates(N):
+        try:
+            k = api.make_knobs(strategy, N, **kw)
+            ms = time_candidate(A, B, strategy, k, iters)
+        except Exception:  # a tuple the geometry rejects for this shape
+            continue
+        res.append((ms, strategy, k.as_dict()))
+    res.sort(key=lambda r: r[0])
+    return res
+
+
+def best(A: api.CsrMatrix, N: int, B: Optional[torch.Tensor] = None, measure: bool = True) -> tuple[str, SsKnobs]:
+    """(strategy, knobs) for A at width N: cached, else measured (or heuristic)."""
+    f = features(A)
+    key = signature(A, N, f)
+    with _LOCK:
+        hit = _MEM.get(key) or _load_disk().get(key)
+    if hit is None:
+        if measure:
+            ranked = tune(A, N, B)
+            strategy, kw = ranked[0][1], ranked[0][2]
+            hit = {"strategy": strategy, "knobs": kw, "ms": ranked[0][0]}
+        else:
+            strategy, kw = heuristic(f, N)
+            hit = {"strategy": strategy, "knobs": api.make_knobs(strategy, N, **kw).as_dict()}
+        with _LOCK:
+            _MEM[key] = hit
+        if measure:
+            _store_disk(key, hit)
+    k = SsKnobs()
+    for name, v in hit["knobs"].items():
+        setattr(k, name, int(v))
+    return hit["strategy"], k

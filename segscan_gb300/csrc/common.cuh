@@ -1,0 +1,226 @@
+// Device helpers shared by every kernel of the library: element types,
+// 2..16-byte vector loads and stores with L2 eviction-priority policies, and
+// the row search whose semantics the reference fixes.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/segscan_gb300.h"
+
+namespace ss {
+
+// ------------------------------------------------------------------
+// Element conversions (storage type <-> FP32 arithmetic)
+// ------------------------------------------------------------------
+template <typename T> struct Elem;
+template <> struct Elem<float> {
+  static __device__ __forceinline__ float to_f(float x) { return x; }
+  static __device__ __forceinline__ float from_f(float x) { return x; }
+};
+template <> struct Elem<__nv_bfloat16> {
+  static __device__ __forceinline__ float to_f(__nv_bfloat16 x) { return __bfloat162float(x); }
+  static __device__ __forceinline__ __nv_bfloat16 from_f(float x) { return __float2bfloat16_rn(x); }
+};
+template <> struct Elem<__half> {
+  static __device__ __forceinline__ float to_f(__half x) { return __half2float(x); }
+  static __device__ __forceinline__ __half from_f(float x) { return __float2half_rn(x); }
+};
+
+// ------------------------------------------------------------------
+// L2 cache policies.  B rows are gathered repeatedly: keep them
+// (evict_last).  The A streams and C are touched once: evict first so they
+// do not push B out of L2.
+// ------------------------------------------------------------------
+__device__ __forceinline__ uint64_t policy_keep() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_stream() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// Raw read-only loads of 2/4/8/16 bytes with an L2 policy.
+__device__ __forceinline__ uint16_t ld_u16(const void *p, uint64_t pol) {
+  uint16_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_u32(const void *p, uint64_t pol) {
+  uint32_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint2 ld_u64(const void *p, uint64_t pol) {
+  uint2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+               : "=r"(v.x), "=r"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint4 ld_u128(const void *p, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
+  return v;
+}
+// Plain int loads for the index streams (A's columns, segment ids, indptr).
+__device__ __forceinline__ int32_t ld_idx(const int32_t *p, uint64_t pol) {
+  return (int32_t)ld_u32(p, pol);
+}
+
+__device__ __forceinline__ void st_u32(void *p, uint32_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_u16(void *p, uint16_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.u16 [%0], %1, %2;" ::"l"(p), "h"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_u64(void *p, uint2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(p), "r"(v.x), "r"(v.y),
+               "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_u128(void *p, uint4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol) : "memory");
+}
+
+// ------------------------------------------------------------------
+// Vector of V elements of T at p (V*sizeof(T) bytes, naturally aligned),
+// widened to FP32.
+// ------------------------------------------------------------------
+__device__ __forceinline__ float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+__device__ __forceinline__ void unpack2(uint32_t u, float &a, float &b, __nv_bfloat16 *) {
+  a = bf16_lo(u);
+  b = bf16_hi(u);
+}
+__device__ __forceinline__ void unpack2(uint32_t u, float &a, float &b, __half *) {
+  __half2 h = *reinterpret_cast<__half2 *>(&u);
+  float2 f = __half22float2(h);
+  a = f.x;
+  b = f.y;
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void load_vec(const T *p, float (&out)[V], uint64_t pol) {
+  constexpr int BYTES = V * (int)sizeof(T);
+  static_assert(BYTES <= 16, "vector wider than 16 bytes");
+  if constexpr (sizeof(T) == 4) {
+    if constexpr (V == 4) {
+      uint4 u = ld_u128(p, pol);
+      out[0] = __uint_as_float(u.x); out[1] = __uint_as_float(u.y);
+      out[2] = __uint_as_float(u.z); out[3] = __uint_as_float(u.w);
+    } else if constexpr (V == 2) {
+      uint2 u = ld_u64(p, pol);
+      out[0] = __uint_as_float(u.x); out[1] = __uint_as_float(u.y);
+    } else {
+      out[0] = __uint_as_float(ld_u32(p, pol));
+    }
+  } else {
+    if constexpr (V == 8) {
+      uint4 u = ld_u128(p, pol);
+      unpack2(u.x, out[0], out[1], (T *)nullptr); unpack2(u.y, out[2], out[3], (T *)nullptr);
+      unpack2(u.z, out[4], out[5], (T *)nullptr); unpack2(u.w, out[6], out[7], (T *)nullptr);
+    } else if constexpr (V == 4) {
+      uint2 u = ld_u64(p, pol);
+      unpack2(u.x, out[0], out[1], (T *)nullptr); unpack2(u.y, out[2], out[3], (T *)nullptr);
+    } else if constexpr (V == 2) {
+      uint32_t u = ld_u32(p, pol);
+      unpack2(u, out[0], out[1], (T *)nullptr);
+    } else {
+      uint16_t h = ld_u16(p, pol);
+      out[0] = Elem<T>::to_f(*reinterpret_cast<T *>(&h));
+    }
+  }
+}
+
+// One scalar value of A (values == nullptr means 1, the reference's
+// __guard_load_default_one, test-cg/include/util/check.cuh:104-111).
+template <typename T>
+__device__ __forceinline__ float load_val(const T *vals, int64_t p, uint64_t pol) {
+  if (vals == nullptr) return 1.0f;
+  if constexpr (sizeof(T) == 4) {
+    return __uint_as_float(ld_u32(vals + p, pol));
+  } else {
+    uint16_t h = ld_u16(vals + p, pol);
+    return Elem<T>::to_f(*reinterpret_cast<T *>(&h));
+  }
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b, __nv_bfloat16 *) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+__device__ __forceinline__ uint32_t pack2(float a, float b, __half *) {
+  __half2 h = __floats2half2_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void store_vec(T *p, const float (&v)[V], uint64_t pol) {
+  if constexpr (sizeof(T) == 4) {
+    if constexpr (V == 4) {
+      st_u128(p, make_uint4(__float_as_uint(v[0]), __float_as_uint(v[1]), __float_as_uint(v[2]),
+                            __float_as_uint(v[3])), pol);
+    } else if constexpr (V == 2) {
+      st_u64(p, make_uint2(__float_as_uint(v[0]), __float_as_uint(v[1])), pol);
+    } else {
+      st_u32(p, __float_as_uint(v[0]), pol);
+    }
+  } else {
+    if constexpr (V == 8) {
+      st_u128(p, make_uint4(pack2(v[0], v[1], (T *)nullptr), pack2(v[2], v[3], (T *)nullptr),
+                            pack2(v[4], v[5], (T *)nullptr), pack2(v[6], v[7], (T *)nullptr)), pol);
+    } else if constexpr (V == 4) {
+      st_u64(p, make_uint2(pack2(v[0], v[1], (T *)nullptr), pack2(v[2], v[3], (T *)nullptr)), pol);
+    } else if constexpr (V == 2) {
+      st_u32(p, pack2(v[0], v[1], (T *)nullptr), pol);
+    } else {
+      T h = Elem<T>::from_f(v[0]);
+      st_u16(p, *reinterpret_cast<uint16_t *>(&h), pol);
+    }
+  }
+}
+
+// Plain (coherent) vector load of the output, for accumulate mode.
+template <typename T, int V>
+__device__ __forceinline__ void load_out(const T *p, float (&out)[V]) {
+  #pragma unroll
+  for (int i = 0; i < V; i++) out[i] = Elem<T>::to_f(p[i]);
+}
+
+// ------------------------------------------------------------------
+// Row of nonzero e: upper_bound(indptr[lo..hi-1], e) - 1 searched over
+// [lo, hi).  With lo = 1, hi = M this is exactly the reference's
+// binary_search_segment_number (test-cg/include/util/check.cuh:88-102):
+// empty rows are skipped and e >= nnz maps to M-1.  Narrowing [lo, hi) to a
+// range known to contain the answer gives the same result in fewer steps.
+// ------------------------------------------------------------------
+__device__ __forceinline__ int row_search(const int32_t *indptr, int lo, int hi, int e) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(indptr + mid) <= e) lo = mid + 1; else hi = mid;
+  }
+  return hi - 1;
+}
+
+// Compensated (Kahan) accumulation step: acc += x with running error c.
+__device__ __forceinline__ void kahan_add(float &acc, float &c, float x) {
+  float y = x - c;
+  float t = acc + y;
+  c = (t - acc) - y;
+  acc = t;
+}
+
+// Lane mask of the aligned sub-warp of `width` lanes containing this lane.
+__device__ __forceinline__ unsigned team_mask(int width) {
+  if (width >= 32) return 0xffffffffu;
+  unsigned lane = threadIdx.x & 31u;  // callers keep teams inside one warp
+  unsigned base = lane & ~(unsigned)(width - 1);
+  return ((1u << width) - 1u) << base;
+}
+
+}  // namespace ss

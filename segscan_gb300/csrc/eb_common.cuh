@@ -1,0 +1,136 @@
+// Element-balanced machinery shared by the sequential (ebsr, segment SR) and
+// parallel (ebpr, segment PR) kernels.
+//
+// Work is cut into chunks of consecutive nonzeros.  A row is OWNED by the
+// chunk that holds its first nonzero; the owner writes the row with plain
+// stores.  A row that started in an earlier chunk (the chunk's HEAD row)
+// continues into this chunk; its partial goes to the chunk's carry slot and
+// a fix-up pass adds it to the owner's value afterwards.  Empty rows (empty
+// segments) are written as zero by the chunk holding the next nonzero, so in
+// overwrite mode every output row is written exactly once, no zero fill and
+// no atomics are needed, and the result is deterministic.  This replaces the
+// reference's per-segment atomicAdd into a pre-zeroed C
+// (test-cg/include/spmm/spmm_cg.cuh:80,104,466,474; new-cg/include/segscan/
+// segscan.cuh:58,77,452,459).
+#pragma once
+#include <climits>
+
+#include "common.cuh"
+
+namespace ss {
+
+struct EbArgs {
+  int M;  // rows of C (SpMM) or dst_len (segment)
+  int K, N, nnz;
+  const int32_t *indptr;  // SpMM: A's row pointer
+  const int32_t *cols;    // SpMM: A's column indices
+  const int32_t *index;   // segment: sorted segment ids
+  const void *vals;       // SpMM: A's values (null = ones)
+  const void *B;          // SpMM: B; segment: src
+  void *C;
+  int accumulate, reduce, kahan;
+  int team_lanes, log2_team_lanes;
+  int colgroups, log2_colgroups;  // pr kernels: column groups per worker
+  int col_tile;
+  int chunk, num_chunks, workers_per_block, stage;
+  int32_t *carry_rows;
+  float *carry_vals;
+};
+
+struct ChunkInfo {
+  int cs, ce;        // nonzero range [cs, ce)
+  int r_first;       // row of nonzero cs
+  int r_last;        // row of nonzero ce - 1
+  int prev_row;      // row of nonzero cs - 1 (-1 when cs == 0)
+  bool has_head;     // r_first started before cs
+};
+
+template <bool SEG>
+__device__ __forceinline__ ChunkInfo chunk_info(const EbArgs &a, int chunk) {
+  ChunkInfo ci;
+  ci.cs = chunk * a.chunk;
+  ci.ce = min(ci.cs + a.chunk, a.nnz);
+  if (SEG) {
+    ci.r_first = __ldg(a.index + ci.cs);
+    ci.r_last = __ldg(a.index + ci.ce - 1);
+    ci.prev_row = ci.cs > 0 ? __ldg(a.index + ci.cs - 1) : -1;
+    ci.has_head = ci.cs > 0 && ci.prev_row == ci.r_first;
+  } else {
+    // binary_search_segment_number semantics (check.cuh:88-102)
+    ci.r_first = row_search(a.indptr, 1, a.M, ci.cs);
+    ci.r_last = row_search(a.indptr, 1, a.M, ci.ce - 1);
+    ci.has_head = ci.cs > 0 && __ldg(a.indptr + ci.r_first) < ci.cs;
+    ci.prev_row = ci.cs == 0 ? -1 : (ci.has_head ? ci.r_first : row_search(a.indptr, 1, a.M, ci.cs - 1));
+  }
+  return ci;
+}
+
+// Row (segment) of nonzero p inside a chunk whose rows span [r_first, r_last].
+template <bool SEG>
+__device__ __forceinline__ int chunk_row(const EbArgs &a, const ChunkInfo &ci, int p) {
+  if (SEG) return __ldg(a.index + p);
+  return row_search(a.indptr, ci.r_first + 1, ci.r_last + 1, p);
+}
+
+// Does the chunk's last row end inside the chunk?
+template <bool SEG>
+__device__ __forceinline__ bool row_ends_in_chunk(const EbArgs &a, const ChunkInfo &ci, int row) {
+  if (ci.ce >= a.nnz) return true;
+  if (SEG) return __ldg(a.index + ci.ce) != row;
+  if ((unsigned)row >= (unsigned)a.M) return true;
+  return __ldg(a.indptr + row + 1) <= ci.ce;
+}
+
+// Writes zeros to rows [lo, hi] (clamped to the output) for this lane's
+// columns.  Used only in overwrite mode.
+template <typename TC, int V, int NV>
+__device__ __forceinline__ void zero_rows(const EbArgs &a, int lo, int hi, int col0,
+                                          const bool (&act)[NV], uint64_t pol) {
+  lo = max(lo, 0);
+  hi = min(hi, a.M - 1);
+  float z[V];
+  #pragma unroll
+  for (int i = 0; i < V; i++) z[i] = 0.f;
+  TC *C = (TC *)a.C;
+  for (int r = lo; r <= hi; r++)
+    #pragma unroll
+    for (int j = 0; j < NV; j++)
+      if (act[j]) store_vec<TC, V>(C + (int64_t)r * a.N + col0 + j * V, z, pol);
+}
+
+// Writes one finished row partial: to the carry slot when it is the chunk's
+// head row, else to C (the owner).  `complete` = the row ends in this chunk.
+template <typename TC, int V, int NV>
+__device__ __forceinline__ void flush_row(const EbArgs &a, const ChunkInfo &ci, int chunk, int row,
+                                          float (&acc)[NV][V], int cnt, bool complete, int col0,
+                                          const bool (&act)[NV], uint64_t pol) {
+  if (ci.has_head && row == ci.r_first) {
+    #pragma unroll
+    for (int j = 0; j < NV; j++)
+      if (act[j]) store_vec<float, V>(a.carry_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], pol);
+    return;
+  }
+  if ((unsigned)row >= (unsigned)a.M) return;
+  TC *C = (TC *)a.C;
+  #pragma unroll
+  for (int j = 0; j < NV; j++) {
+    if (!act[j]) continue;
+    float out[V];
+    #pragma unroll
+    for (int i = 0; i < V; i++) out[i] = acc[j][i];
+    if (a.reduce == SS_MEAN && complete) {
+      #pragma unroll
+      for (int i = 0; i < V; i++) out[i] = acc[j][i] / (float)cnt;
+    }
+    TC *dst = C + (int64_t)row * a.N + col0 + j * V;
+    if (a.accumulate) {
+      float prev[V];
+      load_out<TC, V>(dst, prev);
+      #pragma unroll
+      for (int i = 0; i < V; i++) out[i] += prev[i];
+    }
+    store_vec<TC, V>(dst, out, pol);
+  }
+}
+
+}  // namespace ss

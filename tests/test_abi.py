@@ -1,0 +1,82 @@
+"""The C-ABI library loads, exports every symbol include/*.h declares, and
+rejects bad arguments on the host (no GPU needed)."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+import segscan_gb300
+from segscan_gb300 import _lib
+from segscan_gb300._lib import SsCsr, SsKnobs, Status
+
+HEADERS = sorted((Path(__file__).resolve().parent.parent / "include").glob("*.h"))
+
+
+def declared_symbols():
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(ss_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_symbols()
+    assert len(names) >= 20
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+    assert names <= set(_lib.symbols())
+
+
+def test_version_and_status_strings(lib):
+    assert lib.ss_version() >= 1
+    assert lib.ss_status_string(0) == b"ok"
+    assert lib.ss_status_string(Status.UNSUPPORTED_KNOBS) == b"unsupported knob tuple"
+
+
+@pytest.mark.parametrize("strategy", range(4))
+def test_default_knobs(lib, strategy):
+    k = SsKnobs()
+    assert lib.ss_default_knobs(strategy, 64, ctypes.byref(k)) == 0
+    assert k.thread_per_block == 256 and k.block_numer >= 1 and k.block_denom >= 1
+
+
+def fake_csr(nrow=100, ncol=100, nnz=1000):
+    # device pointers are never dereferenced by the size/argument checks
+    return SsCsr(nrow, ncol, nnz, 256, 512, 1024, 0)
+
+
+def test_workspace_size_queries(lib):
+    A = fake_csr()
+    n = ctypes.c_size_t()
+    for strategy in (1, 3):  # row-balanced strategies need no scratch
+        assert lib.ss_spmm_workspace_size(strategy, ctypes.byref(A), 64, None, ctypes.byref(n)) == 0
+        assert n.value == 0
+    for strategy in (0, 2):
+        assert lib.ss_spmm_workspace_size(strategy, ctypes.byref(A), 64, None, ctypes.byref(n)) == 0
+        assert n.value > 0
+    assert lib.ss_segment_coo_workspace_size(1, 1000, 16, None, ctypes.byref(n)) == 0
+    assert n.value > 0
+
+
+def test_bad_arguments_rejected_without_launch(lib):
+    A = fake_csr()
+    n = ctypes.c_size_t()
+    assert lib.ss_spmm(0, None, 4, 1, 1, 0, 0, None, None, 0, None) == Status.INVALID_ARG
+    bad = SsKnobs(9, 9, 256, 1, 1, 4, 1, 0)
+    assert lib.ss_spmm_workspace_size(0, ctypes.byref(A), 64, ctypes.byref(bad), ctypes.byref(n)) == \
+        Status.UNSUPPORTED_KNOBS
+    assert b"tile_factor" in lib.ss_last_error()
+    assert lib.ss_spmm(3, ctypes.byref(A), 64, 4096, 8192, 5, 0, None, None, 0, None) == Status.INVALID_ARG
+    # segment: accumulate only for sums
+    assert lib.ss_segment_coo(1, 4096, 0, 8192, 10, 4, 10, 4096, 1, 1, None, None, 0, None) == \
+        Status.INVALID_ARG
+    # workspace too small for an element-balanced strategy
+    assert lib.ss_spmm(2, ctypes.byref(A), 64, 4096, 8192, 0, 0, None, 4096, 16, None) in \
+        (Status.WORKSPACE, Status.CUDA)
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(ImportError):
+        _lib.load(tmp_path / "nope.so")

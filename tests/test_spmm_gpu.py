@@ -1,0 +1,209 @@
+"""SpMM parity: every strategy against the reference's check path (golden
+fixtures) and the FP64 oracle.  FP32 tolerance: |C - C64| <= 1e-5 * (|A||B|)
+per element and 1e-5 normwise; BF16/FP16 storage: 2e-2 normwise against FP64
+on the FP32 inputs."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+import oracle_lib
+from gpu_util import check_close, dev_csr, oracle64, powerlaw_medium, rounded
+from segscan_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+STRATS = ["ebpr", "rbpr", "ebsr", "rbsr"]
+
+
+def spmm(A, B, strategy, **kw):
+    from segscan_gb300 import api
+    out = api.spmm(A, B, strategy, **kw)
+    torch.cuda.synchronize()
+    return out
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+@pytest.mark.parametrize("name", ["spmm_poisson512_n4.npz", "spmm_poisson512_n16.npz", "spmm_edge_n3.npz"])
+def test_golden(cuda, strategy, name):
+    g = np.load(GOLD / name)
+    csr = synth.Csr(g["indptr"].size - 1, int(g["ncol"]), g["indptr"], g["indices"], g["values"])
+    A = dev_csr(csr)
+    C = spmm(A, torch.from_numpy(g["B"]).cuda(), strategy).cpu().numpy()
+    C64, absC = oracle64(csr, g["B"])
+    check_close(C, C64, absC, 1e-5, 1e-5, f"{strategy} vs FP64")
+    check_close(C, g["C"].astype(np.float64), absC, 2e-5, None, f"{strategy} vs reference check path")
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+def test_ones_known_answer_exact(cuda, strategy):
+    g = np.load(GOLD / "spmm_ones_kat_n8.npz")
+    csr = synth.Csr(g["indptr"].size - 1, int(g["ncol"]), g["indptr"], g["indices"], g["values"])
+    for values in (True, False):  # values=None is the reference's all-ones default
+        A = dev_csr(csr, values=values)
+        C = spmm(A, torch.from_numpy(g["B"]).cuda(), strategy).cpu().numpy()
+        assert np.array_equal(C, g["C"]), strategy
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 16, 33, 64, 128])
+def test_widths(cuda, strategy, N):
+    csr = synth.poisson(700, 900, 9.0, seed=N)
+    B = synth.dense(900, N, seed=N + 1)
+    C = spmm(dev_csr(csr), torch.from_numpy(B).cuda(), strategy).cpu().numpy()
+    C64, absC = oracle64(csr, B)
+    check_close(C, C64, absC, 1e-5, 1e-5, f"{strategy} N={N}")
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+@pytest.mark.parametrize("N", [3, 64])
+def test_powerlaw_long_rows(cuda, strategy, N):
+    csr = powerlaw_medium()
+    B = synth.dense(csr.ncol, N, seed=5)
+    C = spmm(dev_csr(csr), torch.from_numpy(B).cuda(), strategy).cpu().numpy()
+    C64, absC = oracle64(csr, B)
+    check_close(C, C64, absC, 1e-5, 1e-5, f"{strategy} powerlaw N={N}")
+
+
+KNOB_SWEEP = {
+    # README.md:168-210 best static tuples and test-cg/src/params.md grids
+    "ebpr": [dict(group_factor=5, tile_factor=5, block_denom=8), dict(group_factor=4, tile_factor=5, block_denom=4),
+             dict(group_factor=2, tile_factor=2, block_numer=2), dict(group_factor=0, tile_factor=0, block_denom=32)],
+    "rbpr": [dict(group_factor=3, tile_factor=3, block_denom=2), dict(group_factor=2, tile_factor=2, block_denom=1),
+             dict(group_factor=5, tile_factor=5, block_denom=16), dict(group_factor=0, tile_factor=4)],
+    "ebsr": [dict(group_factor=4, coarsen_factor=4, thread_nz=2, block_denom=16),
+             dict(group_factor=3, coarsen_factor=2, thread_nz=1, block_denom=8),
+             dict(group_factor=5, coarsen_factor=1, thread_nz=32, thread_per_block=128),
+             dict(group_factor=0, coarsen_factor=8, thread_nz=64, thread_per_block=64),
+             dict(group_factor=2, coarsen_factor=3, thread_nz=300, thread_per_block=512)],
+    "rbsr": [dict(coarsen_factor=4, tile_factor=5), dict(coarsen_factor=2, tile_factor=1, block_denom=4),
+             dict(coarsen_factor=1, tile_factor=0), dict(coarsen_factor=8, tile_factor=7, thread_per_block=1024)],
+}
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+@pytest.mark.parametrize("N", [5, 48])
+def test_knob_sweep(cuda, strategy, N):
+    from segscan_gb300 import api
+    g = np.load(GOLD / "spmm_edge_n3.npz")
+    csr = synth.Csr(g["indptr"].size - 1, int(g["ncol"]), g["indptr"], g["indices"], g["values"])
+    B = synth.dense(csr.ncol, N, seed=9)
+    C64, absC = oracle64(csr, B)
+    A = dev_csr(csr)
+    for kw in KNOB_SWEEP[strategy]:
+        k = api.make_knobs(strategy, N, **kw)
+        C = spmm(A, torch.from_numpy(B).cuda(), strategy, knobs=k).cpu().numpy()
+        check_close(C, C64, absC, 1e-5, 1e-5, f"{strategy} {kw}")
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("out_f32", [True, False])
+def test_half_storage(cuda, strategy, dtype, out_f32):
+    csr = powerlaw_medium(M=20000, lmax=3000)
+    N = 64
+    B = synth.dense(csr.ncol, N, seed=2)
+    A = dev_csr(csr, dtype)
+    Bd = torch.from_numpy(B).cuda().to(dtype)
+    C = spmm(A, Bd, strategy, out_dtype=torch.float32 if out_f32 else dtype).float().cpu().numpy()
+    C64, absC = oracle64(csr, B)
+    check_close(C, C64, absC, 2e-2 if dtype == torch.bfloat16 else 5e-3, 2e-2, f"{strategy} {dtype} vs FP64(fp32 in)")
+    # against FP64 on the stored (rounded) inputs only accumulation and the
+    # output rounding remain
+    Cr64, absCr = oracle64(csr, rounded(B, dtype), rounded(csr.values, dtype))
+    out_tol = 1e-5 if out_f32 else (8e-3 if dtype == torch.bfloat16 else 1e-3)
+    Cn = np.abs(Cr64) * out_tol + 1e-5 * absCr
+    err = np.abs(C - Cr64)
+    assert np.all(err <= Cn + 1e-30), f"{strategy} {dtype}: worst {err.max():.3e}"
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+def test_accumulate(cuda, strategy):
+    csr = synth.poisson(300, 300, 5.0, seed=4)
+    B = synth.dense(300, 16, seed=4)
+    C0 = synth.dense(300, 16, seed=44)
+    out = torch.from_numpy(C0.copy()).cuda()
+    spmm(dev_csr(csr), torch.from_numpy(B).cuda(), strategy, out=out, accumulate=True)
+    C64, absC = oracle64(csr, B)
+    check_close(out.cpu().numpy(), C64 + C0, absC + np.abs(C0), 1e-5, None, strategy)
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+def test_degenerate_shapes(cuda, strategy):
+    from segscan_gb300 import api
+    # nnz = 0: overwrite mode writes zeros
+    empty = synth.Csr(50, 40, np.zeros(51, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32))
+    out = torch.full((50, 8), 7.0, device="cuda")
+    spmm(dev_csr(empty), torch.ones(40, 8, device="cuda"), strategy, out=out)
+    assert not out.any()
+    # one row
+    one = synth.poisson(1, 5000, 3000.0, seed=1)
+    B = synth.dense(5000, 4, seed=1)
+    C = spmm(dev_csr(one), torch.from_numpy(B).cuda(), strategy).cpu().numpy()
+    C64, absC = oracle64(one, B)
+    check_close(C, C64, absC, 1e-5, None, "M=1")
+    # all rows empty but the last
+    lengths = np.zeros(64, np.int64)
+    lengths[-1] = 10
+    last = synth.csr_from_lengths(64, 64, lengths, np.random.default_rng(0))
+    B = synth.dense(64, 8, seed=2)
+    out = torch.full((64, 8), 3.0, device="cuda")
+    spmm(dev_csr(last), torch.from_numpy(B).cuda(), strategy, out=out)
+    C64, absC = oracle64(last, B)
+    check_close(out.cpu().numpy(), C64, absC, 1e-5, None, "trailing row")
+
+
+def test_reference_named_wrappers(cuda):
+    from segscan_gb300 import api
+    g = np.load(GOLD / "spmm_poisson512_n16.npz")
+    csr = synth.Csr(g["indptr"].size - 1, int(g["ncol"]), g["indptr"], g["indices"], g["values"])
+    A = dev_csr(csr)
+    B = torch.from_numpy(g["B"]).cuda()
+    C64, absC = oracle64(csr, g["B"])
+    calls = [
+        (api.csrspmm_parreduce_nnzbalance_cg, dict(group_factor=5, thread_per_block=256, tile_factor=5,
+                                                    block_numer=1, block_denom=8)),
+        (api.csrspmm_parreduce_rowbalance_cg, dict(group_factor=3, thread_per_block=256, tile_factor=3,
+                                                    block_numer=1, block_denom=2)),
+        (api.csrspmm_rowcaching_nnzbalance_cg, dict(group_factor=4, thread_per_block=256, CoarsenFactor=4,
+                                                     ThreadNz=1, block_numer=1, block_denom=16)),
+        (api.csrspmm_seqreduce_rowbalance_cg, dict(coarsen_factor=4, thread_per_block=256, tile_factor=5,
+                                                    block_numer=1, block_denom=1)),
+    ]
+    for fn, kw in calls:
+        C = torch.zeros(A.nrow, 16, device="cuda")  # the reference's out_feature.reset()
+        fn(A, 16, B, C, **kw)
+        torch.cuda.synchronize()
+        check_close(C.cpu().numpy(), C64, absC, 1e-5, 1e-5, fn.__name__)
+
+
+def test_deterministic(cuda):
+    csr = powerlaw_medium()
+    B = torch.from_numpy(synth.dense(csr.ncol, 32, seed=3)).cuda()
+    A = dev_csr(csr)
+    for strategy in STRATS:
+        c1 = spmm(A, B, strategy)
+        c2 = spmm(A, B, strategy)
+        assert torch.equal(c1, c2), strategy
+
+
+def test_row_ids_bit_exact(cuda):
+    from segscan_gb300 import api
+    g = np.load(GOLD / "row_ids_edge.npz")
+    ip = torch.from_numpy(g["indptr"]).cuda()
+    rows = api.row_ids(ip, int(g["nnz"]), torch.from_numpy(g["elems"]).cuda()).cpu().numpy()
+    assert np.array_equal(rows, g["rows"])
+    big = powerlaw_medium()
+    rows = api.row_ids(torch.from_numpy(big.indptr).cuda(), big.nnz).cpu().numpy()
+    assert np.array_equal(rows, big.coo_rows())
+
+
+def test_validate(cuda):
+    from segscan_gb300 import api
+    csr = synth.poisson(100, 100, 4.0, seed=1)
+    A = dev_csr(csr)
+    assert api.validate(A) == 0
+    bad = A.indices.clone()
+    bad[3] = 1000
+    assert api.validate(api.CsrMatrix(A.nrow, A.ncol, A.indptr, bad, A.values)) & 8
