@@ -106,9 +106,14 @@ __device__ __forceinline__ void unpack2(uint32_t u, float &a, float &b, __half *
 
 template <typename T, int V>
 __device__ __forceinline__ void load_vec(const T *p, float (&out)[V], uint64_t pol) {
-  constexpr int BYTES = V * (int)sizeof(T);
-  static_assert(BYTES <= 16, "vector wider than 16 bytes");
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (V * sizeof(T) > 16) {
+    constexpr int H = V / 2;
+    float lo[H], hi[H];
+    load_vec<T, H>(p, lo, pol);
+    load_vec<T, H>(p + H, hi, pol);
+    #pragma unroll
+    for (int i = 0; i < H; i++) { out[i] = lo[i]; out[H + i] = hi[i]; }
+  } else if constexpr (sizeof(T) == 4) {
     if constexpr (V == 4) {
       uint4 u = ld_u128(p, pol);
       out[0] = __uint_as_float(u.x); out[1] = __uint_as_float(u.y);
@@ -161,7 +166,15 @@ __device__ __forceinline__ uint32_t pack2(float a, float b, __half *) {
 
 template <typename T, int V>
 __device__ __forceinline__ void store_vec(T *p, const float (&v)[V], uint64_t pol) {
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (V * sizeof(T) > 16) {
+    // wider than one 16-byte access (FP32 output of an 8-wide 16-bit vector)
+    constexpr int H = V / 2;
+    float lo[H], hi[H];
+    #pragma unroll
+    for (int i = 0; i < H; i++) { lo[i] = v[i]; hi[i] = v[H + i]; }
+    store_vec<T, H>(p, lo, pol);
+    store_vec<T, H>(p + H, hi, pol);
+  } else if constexpr (sizeof(T) == 4) {
     if constexpr (V == 4) {
       st_u128(p, make_uint4(__float_as_uint(v[0]), __float_as_uint(v[1]), __float_as_uint(v[2]),
                             __float_as_uint(v[3])), pol);

@@ -1,11 +1,12 @@
 // Carry fix-up for the element-balanced kernels (see eb_common.cuh).
 //
-// Chunk c's carry slot holds the partial of its head row r (a row that
+// Chunk c's head slot holds the partial of its head row r (a row that
 // started in an earlier chunk) or -1.  The first chunk of each run of
-// consecutive chunks carrying the same row is the run's leader: it sums the
-// run's carries in chunk order (compensated) and folds them into the value
-// the owner already stored, dividing by the segment length for a mean.  The
-// order is fixed, so results are reproducible bit for bit.
+// consecutive chunks with the same head row is the run's leader; the chunk
+// before it owns r and left r's partial in its tail slot.  The leader sums
+// tail + heads in chunk order (compensated), adds the old output in
+// accumulate mode, divides by the segment length for a mean, and stores the
+// row once.  The order is fixed, so results are reproducible bit for bit.
 #include "eb_common.cuh"
 #include "internal.h"
 
@@ -15,7 +16,7 @@ namespace ss {
 
 size_t eb_workspace_bytes(const EbGeom &g, int N) {
   size_t rows = ((size_t)g.num_chunks * sizeof(int32_t) + 255) & ~(size_t)255;
-  return rows + (size_t)g.num_chunks * (size_t)N * sizeof(float);
+  return rows + 2 * (size_t)g.num_chunks * (size_t)N * sizeof(float);
 }
 
 CarryView carry_view(void *ws, int num_chunks, int N) {
@@ -23,7 +24,7 @@ CarryView carry_view(void *ws, int num_chunks, int N) {
   size_t rows = ((size_t)num_chunks * sizeof(int32_t) + 255) & ~(size_t)255;
   cv.rows = (int32_t *)ws;
   cv.vals = (float *)((char *)ws + rows);
-  (void)N;
+  cv.tails = cv.vals + (size_t)num_chunks * (size_t)N;
   return cv;
 }
 
@@ -42,6 +43,7 @@ EbArgs eb_base_args(const EbGeom &g, void *ws, int N) {
   CarryView cv = carry_view(ws, g.num_chunks, N);
   a.carry_rows = cv.rows;
   a.carry_vals = cv.vals;
+  a.tail_vals = cv.tails;
   return a;
 }
 
@@ -56,15 +58,16 @@ __device__ __forceinline__ int lower_bound_idx(const int32_t *index, int n, int 
 
 template <typename TC>
 __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restrict__ rows,
-                                                          const float *__restrict__ vals, int num_chunks,
-                                                          int N, int M, TC *C, int reduce,
+                                                          const float *__restrict__ heads,
+                                                          const float *__restrict__ tails, int num_chunks,
+                                                          int N, int M, TC *C, int reduce, int accumulate,
                                                           const int32_t *__restrict__ index, int nnz) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += warps) {
     const int r = rows[c];
-    if (r < 0 || r >= M) continue;
-    if (c > 0 && rows[c - 1] == r) continue;  // not the leader of this run
+    if (c == 0 || r < 0 || r >= M) continue;
+    if (rows[c - 1] == r) continue;  // not the leader of this run
     int cend = c + 1;
     while (cend < num_chunks && rows[cend] == r) cend++;
     float count = 1.f;
@@ -80,13 +83,14 @@ __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restr
     }
     TC *crow = C + (int64_t)r * N;
     for (int j = lane; j < N; j += 32) {
-      float acc = Elem<TC>::to_f(crow[j]);
+      float acc = tails[(int64_t)(c - 1) * N + j];  // the owner's partial
       float comp = 0.f;
       for (int k = c; k < cend; k++) {
-        const float x = vals[(int64_t)k * N + j];
+        const float x = heads[(int64_t)k * N + j];
         if (reduce == SS_MAX) acc = fmaxf(acc, x);
         else kahan_add(acc, comp, x);
       }
+      if (accumulate) acc += Elem<TC>::to_f(crow[j]);
       if (reduce == SS_MEAN) acc = acc / count;
       crow[j] = Elem<TC>::from_f(acc);
     }
@@ -94,19 +98,20 @@ __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restr
 }
 
 ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *C, int c_dtype,
-                       int reduce, const int32_t *index, int nnz, cudaStream_t s) {
+                       int reduce, int accumulate, const int32_t *index, int nnz, cudaStream_t s) {
   if (num_chunks <= 1 || N == 0 || M == 0) return SS_OK;  // chunk 0 never carries
   const int threads = 256;
   const int blocks = std::max(1, std::min((num_chunks + 7) / 8, 152 * 32));
   if (c_dtype == SS_F32)
-    carry_fixup_kernel<float><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, num_chunks, N, M, (float *)C,
-                                                          reduce, index, nnz);
+    carry_fixup_kernel<float><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, cv.tails, num_chunks, N, M,
+                                                          (float *)C, reduce, accumulate, index, nnz);
   else if (c_dtype == SS_BF16)
-    carry_fixup_kernel<__nv_bfloat16><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, num_chunks, N, M,
-                                                                  (__nv_bfloat16 *)C, reduce, index, nnz);
+    carry_fixup_kernel<__nv_bfloat16><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, cv.tails, num_chunks, N,
+                                                                  M, (__nv_bfloat16 *)C, reduce, accumulate,
+                                                                  index, nnz);
   else
-    carry_fixup_kernel<__half><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, num_chunks, N, M, (__half *)C,
-                                                           reduce, index, nnz);
+    carry_fixup_kernel<__half><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, cv.tails, num_chunks, N, M,
+                                                           (__half *)C, reduce, accumulate, index, nnz);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return cuda_fail(err, "carry fix-up launch");
   return SS_OK;

@@ -3,9 +3,12 @@
 //
 // Work is cut into chunks of consecutive nonzeros.  A row is OWNED by the
 // chunk that holds its first nonzero; the owner writes the row with plain
-// stores.  A row that started in an earlier chunk (the chunk's HEAD row)
-// continues into this chunk; its partial goes to the chunk's carry slot and
-// a fix-up pass adds it to the owner's value afterwards.  Empty rows (empty
+// stores when the row also ends in that chunk.  Only two rows of a chunk can
+// straddle a chunk boundary: the HEAD row (started in an earlier chunk) and
+// the last row (continues into the next chunk).  Their FP32 partials go to
+// the chunk's head and tail slots, and a fix-up pass assembles each
+// straddling row as owner tail + following heads and stores it once, so a
+// 16-bit output is rounded once.  Empty rows (empty
 // segments) are written as zero by the chunk holding the next nonzero, so in
 // overwrite mode every output row is written exactly once, no zero fill and
 // no atomics are needed, and the result is deterministic.  This replaces the
@@ -33,8 +36,9 @@ struct EbArgs {
   int colgroups, log2_colgroups;  // pr kernels: column groups per worker
   int col_tile;
   int chunk, num_chunks, workers_per_block, stage;
-  int32_t *carry_rows;
-  float *carry_vals;
+  int32_t *carry_rows;  // [num_chunks] head row of each chunk, -1 = none
+  float *carry_vals;    // [num_chunks * N] head-row partials
+  float *tail_vals;     // [num_chunks * N] partial of a last row that continues
 };
 
 struct ChunkInfo {
@@ -98,8 +102,9 @@ __device__ __forceinline__ void zero_rows(const EbArgs &a, int lo, int hi, int c
       if (act[j]) store_vec<TC, V>(C + (int64_t)r * a.N + col0 + j * V, z, pol);
 }
 
-// Writes one finished row partial: to the carry slot when it is the chunk's
-// head row, else to C (the owner).  `complete` = the row ends in this chunk.
+// Writes one row partial: to the head slot when it is the chunk's head row,
+// to the tail slot when the row continues past the chunk (`complete` false),
+// else to C (the owner of a row that starts and ends in this chunk).
 template <typename TC, int V, int NV>
 __device__ __forceinline__ void flush_row(const EbArgs &a, const ChunkInfo &ci, int chunk, int row,
                                           float (&acc)[NV][V], int cnt, bool complete, int col0,
@@ -110,6 +115,12 @@ __device__ __forceinline__ void flush_row(const EbArgs &a, const ChunkInfo &ci, 
       if (act[j]) store_vec<float, V>(a.carry_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], pol);
     return;
   }
+  if (!complete) {
+    #pragma unroll
+    for (int j = 0; j < NV; j++)
+      if (act[j]) store_vec<float, V>(a.tail_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], pol);
+    return;
+  }
   if ((unsigned)row >= (unsigned)a.M) return;
   TC *C = (TC *)a.C;
   #pragma unroll
@@ -118,7 +129,7 @@ __device__ __forceinline__ void flush_row(const EbArgs &a, const ChunkInfo &ci, 
     float out[V];
     #pragma unroll
     for (int i = 0; i < V; i++) out[i] = acc[j][i];
-    if (a.reduce == SS_MEAN && complete) {
+    if (a.reduce == SS_MEAN) {
       #pragma unroll
       for (int i = 0; i < V; i++) out[i] = acc[j][i] / (float)cnt;
     }

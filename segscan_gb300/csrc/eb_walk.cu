@@ -182,7 +182,7 @@ ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
                              : sr_ptr<__half, __half, false>(g.cs.V, g.cs.NV);
   ss_status st = run_sr(fn, a, g, s, "ebsr launch");
   if (st != SS_OK) return st;
-  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.M, c.C, c.c_dtype, SS_SUM,
+  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.M, c.C, c.c_dtype, SS_SUM, c.accumulate,
                       nullptr, c.nnz, s);
 }
 
@@ -197,7 +197,7 @@ ss_status launch_seg_sr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_
   else fn = sr_ptr<__half, float, true>(g.cs.V, g.cs.NV);
   ss_status st = run_sr(fn, a, g, s, "segment_coo sr launch");
   if (st != SS_OK) return st;
-  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce,
+  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce, c.accumulate,
                       c.index, c.nnz, s);
 }
 

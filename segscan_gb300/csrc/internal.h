@@ -84,12 +84,13 @@ ss_status launch_seg_pr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_
 
 // Carry fix-up shared by the element-balanced kernels (eb_common.cu).
 struct CarryView {
-  int32_t *rows;   // [num_chunks], -1 = no carry
-  float *vals;     // [num_chunks * N]
+  int32_t *rows;   // [num_chunks], -1 = no head row
+  float *vals;     // [num_chunks * N] head-row partials
+  float *tails;    // [num_chunks * N] partials of rows continuing past a chunk
 };
 CarryView carry_view(void *ws, int num_chunks, int N);
 ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *C, int c_dtype,
-                       int reduce, const int32_t *index, int nnz, cudaStream_t s);
+                       int reduce, int accumulate, const int32_t *index, int nnz, cudaStream_t s);
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 inline int floor_pow2(int x) {

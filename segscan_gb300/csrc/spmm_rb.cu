@@ -216,7 +216,8 @@ __global__ void __launch_bounds__(1024) rbpr_kernel(RbArgs a) {
   for (int j = 0; j < NV; j++) act[j] = col0 + j * V < a.N;
   const uint64_t keep = policy_keep(), strm = policy_stream();
   const int stride = gridDim.x * a.teams_per_block;
-  const int warps_in_team = a.team_threads >> 5;  // 0 when the team fits in one warp
+  // warps a team spans; 0 when the team fits in one warp (no shared memory then)
+  const int warps_in_team = a.team_threads > 32 ? a.team_threads >> 5 : 0;
   for (int row = blockIdx.x * a.teams_per_block + team; row < a.M; row += stride) {
     int s, e;
     clamp_row(a, row, s, e);

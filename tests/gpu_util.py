@@ -16,10 +16,10 @@ def rounded(x, dtype):
     return torch.from_numpy(np.ascontiguousarray(x)).to(dtype).float().numpy()
 
 
-def check_close(C, C64, absC, rtol, normwise=None, what=""):
+def check_close(C, C64, absC, rtol, normwise=None, what="", atol=1e-30):
     C = np.asarray(C, dtype=np.float64)
     err = np.abs(C - C64)
-    bound = rtol * absC + 1e-30
+    bound = rtol * absC + atol
     bad = err > bound
     assert not bad.any(), (f"{what}: {bad.sum()} elements off; worst err {err.max():.3e} "
                            f"at {np.unravel_index(np.argmax(err - bound), err.shape)}")
