@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--N", type=int, default=64)
     ap.add_argument("--strategy", default="auto")
+    ap.add_argument("--knobs", default=None, help="JSON knob overrides for --strategy")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -210,7 +211,8 @@ def run_reference(args):
 def choose(args, A_dev, N):
     from segscan_gb300 import api, autotune
     if args.strategy != "auto":
-        return args.strategy, api.default_knobs(args.strategy, N)
+        kw = json.loads(args.knobs) if args.knobs else {}
+        return args.strategy, api.make_knobs(args.strategy, N, **kw)
     return autotune.best(A_dev, N)
 
 
@@ -290,16 +292,18 @@ def run_ours(args):
         api.spmm(Ae, d_B, strategy, knobs=knobs, out=C, workspace=work, stream=stream)
         h_C.copy_(C, non_blocking=True)
 
-    for _ in range(2):
-        e2e_step()
-    torch.cuda.synchronize(dev)
-    barrier()
-    e0.record(stream)
-    for _ in range(args.e2e_steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    t_e2e = e0.elapsed_time(e1) / 1e3 / args.e2e_steps
+    t_e2e = float("nan")
+    if args.e2e_steps > 0:
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_e2e = e0.elapsed_time(e1) / 1e3 / args.e2e_steps
     if ws_ > 1:
         import torch.distributed as dist
         tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
