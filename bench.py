@@ -42,7 +42,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--N", type=int, default=64)
     ap.add_argument("--strategy", default="auto")
-    ap.add_argument("--knobs", default=None, help="JSON knob overrides for --strategy")
+    ap.add_argument("--knobs", default=None,
+                    help="knob overrides for --strategy: JSON or name=value:name=value")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -211,7 +212,12 @@ def run_reference(args):
 def choose(args, A_dev, N):
     from segscan_gb300 import api, autotune
     if args.strategy != "auto":
-        kw = json.loads(args.knobs) if args.knobs else {}
+        kw = {}
+        if args.knobs:
+            if args.knobs.lstrip().startswith("{"):
+                kw = json.loads(args.knobs)
+            else:
+                kw = {k: int(v) for k, v in (item.split("=") for item in args.knobs.split(":") if item)}
         return args.strategy, api.make_knobs(args.strategy, N, **kw)
     return autotune.best(A_dev, N)
 
