@@ -114,6 +114,11 @@ int ss_version(void);                      /* major * 100 + minor */
 const char *ss_status_string(int status);  /* static string */
 /* Text of the last failure on the calling host thread ("" if none). */
 const char *ss_last_error(void);
+/* Device-side status of the bounded waits in the kernels: *status gets 0 or
+ * SS_ERR_TIMEOUT (a wait gave up and its chunk was skipped).  clear = 1
+ * resets it.  Synchronous with respect to the device.  No counterpart in the
+ * reference (its kernels never wait). */
+ss_status ss_device_error(int *status, int clear);
 /* Knob tuple the reference's README reports as best static choice for a
  * strategy (test-cg README.md:168-210), used when knobs == NULL. */
 ss_status ss_default_knobs(int strategy, int N, ss_knobs *out);

@@ -78,6 +78,7 @@ _SIGNATURES = {
     "ss_status_string": (c_char_p, [c_int]),
     "ss_last_error": (c_char_p, []),
     "ss_default_knobs": (c_int, [c_int, c_int, POINTER(SsKnobs)]),
+    "ss_device_error": (c_int, [POINTER(c_int), c_int]),
     "ss_spmm_workspace_size": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(SsKnobs), POINTER(c_size_t)]),
     "ss_spmm_ebpr": (c_int, [POINTER(SsCsr), c_int, c_void_p, c_void_p, c_int, c_int, POINTER(SsKnobs),
                              c_void_p, c_size_t, c_void_p]),

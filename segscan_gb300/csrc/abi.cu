@@ -140,7 +140,8 @@ static void finish_eb(long long worker_cap, EbGeom &g) {
 
 // ebsr: csrspmm_rowcaching_nnzbalance_cg (spmm_cg.cuh:553-566) and
 // segment_coo_sr / _noshmem_sr / _noshmem_lessatom_sr (segscan.cuh:817-829).
-static ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, const ss_knobs &k, EbGeom &g) {
+static ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_bytes, const ss_knobs &k,
+                         EbGeom &g) {
   ss_status st = check_common_knobs(k);
   if (st) return st;
   if (k.group_factor < 0 || k.group_factor > 5)
@@ -150,6 +151,9 @@ static ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, cons
   if (k.thread_nz < 1 || k.thread_nz > 4096)
     return fail(SS_ERR_UNSUPPORTED_KNOBS, "ThreadNz %d outside [1, 4096]", k.thread_nz);
   const int G = 1 << k.group_factor;
+  if (k.thread_per_block > 512)
+    return fail(SS_ERR_UNSUPPORTED_KNOBS, "sequential-walk blocks hold at most 512 threads (got %d)",
+                k.thread_per_block);
   if (k.thread_per_block % G != 0)
     return fail(SS_ERR_UNSUPPORTED_KNOBS, "thread_per_block %d not a multiple of group size %d",
                 k.thread_per_block, G);
@@ -162,12 +166,16 @@ static ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, cons
   g.block = k.thread_per_block;
   g.chunk = k.thread_nz * G;
   g.num_chunks = nnz > 0 ? ceil_div(nnz, g.chunk) : 0;
-  int stage = g.chunk < 256 ? g.chunk : 256;
-  int cap = 49152 / (12 * g.workers_per_block);
-  if (stage > cap) stage = cap;
-  if (stage < 1) stage = 1;
+  // staged tile: 64 nonzeros, smaller when the block's groups would need
+  // more than 48 KB of shared memory (a multiple of 8 keeps bulk copies
+  // 16-byte aligned)
+  int stage = 64;
+  while (stage > 8 && sr_smem_bytes(stage, g.workers_per_block, val_bytes) > 48 * 1024) stage >>= 1;
   g.stage = stage;
-  g.smem = (size_t)g.workers_per_block * stage * 12;
+  g.smem = sr_smem_bytes(stage, g.workers_per_block, val_bytes);
+  if (g.smem > 200 * 1024)
+    return fail(SS_ERR_UNSUPPORTED_KNOBS, "%d groups per block need %zu B of shared memory",
+                g.workers_per_block, g.smem);
   // reference grid: worker_units * block_factor blocks of thread_per_block
   finish_eb(workers_from_factor(worker_units, k) * g.workers_per_block, g);
   return SS_OK;
@@ -258,7 +266,7 @@ static ss_status spmm_geometry(int strategy, const SpmmCall &c, const ss_knobs &
   switch (strategy) {
     case SS_RBSR: return geom_rbsr(c.M, c.N, c.val_dtype, k, rg);
     case SS_RBPR: return geom_rbpr(c.M, c.N, c.val_dtype, k, rg);
-    case SS_EBSR: return geom_sr(c.M, c.nnz, c.N, c.val_dtype, k, eg);
+    case SS_EBSR: return geom_sr(c.M, c.nnz, c.N, c.val_dtype, dtype_size(c.val_dtype), k, eg);
     case SS_EBPR: return geom_pr(c.M, c.nnz, c.N, c.val_dtype, k, eg);
   }
   return fail(SS_ERR_INVALID_ARG, "unknown strategy %d", strategy);
@@ -388,7 +396,7 @@ ss_status ss_spmm_rbsr(const ss_csr *A, int N, const void *B, void *C, int c_dty
 // segment_coo
 // ---------------------------------------------------------------------
 static ss_status seg_geometry(int seg_strategy, int nnz, int N, int dtype, const ss_knobs &k, EbGeom &g) {
-  if (seg_strategy == SS_SEG_SR) return geom_sr(nnz, nnz, N, dtype, k, g);
+  if (seg_strategy == SS_SEG_SR) return geom_sr(nnz, nnz, N, dtype, 0, k, g);
   if (seg_strategy == SS_SEG_PR) return geom_pr(nnz, nnz, N, dtype, k, g);
   return fail(SS_ERR_INVALID_ARG, "unknown segment strategy %d", seg_strategy);
 }

@@ -33,37 +33,43 @@ template <> struct Elem<__half> {
 // (evict_last).  The A streams and C are touched once: evict first so they
 // do not push B out of L2.
 // ------------------------------------------------------------------
+#ifndef SS_KEEP_FRACTION
+#define SS_KEEP_FRACTION 1.0
+#endif
+#define SS_STR2(x) #x
+#define SS_STR(x) SS_STR2(x)
 __device__ __forceinline__ uint64_t policy_keep() {
   uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  asm("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, " SS_STR(SS_KEEP_FRACTION) ";"
+      : "=l"(p));
   return p;
 }
 __device__ __forceinline__ uint64_t policy_stream() {
   uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
   return p;
 }
 
 // Raw read-only loads of 2/4/8/16 bytes with an L2 policy.
 __device__ __forceinline__ uint16_t ld_u16(const void *p, uint64_t pol) {
   uint16_t v;
-  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
   return v;
 }
 __device__ __forceinline__ uint32_t ld_u32(const void *p, uint64_t pol) {
   uint32_t v;
-  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
   return v;
 }
 __device__ __forceinline__ uint2 ld_u64(const void *p, uint64_t pol) {
   uint2 v;
-  asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+  asm("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
                : "=r"(v.x), "=r"(v.y) : "l"(p), "l"(pol));
   return v;
 }
 __device__ __forceinline__ uint4 ld_u128(const void *p, uint64_t pol) {
   uint4 v;
-  asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+  asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
                : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
   return v;
 }
@@ -218,6 +224,40 @@ __device__ __forceinline__ int row_search(const int32_t *indptr, int lo, int hi,
     if (__ldg(indptr + mid) <= e) lo = mid + 1; else hi = mid;
   }
   return hi - 1;
+}
+
+// ------------------------------------------------------------------
+// Bulk (TMA) copies global -> shared completed on an mbarrier.
+// ------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// dst, src 16-byte aligned; bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
 }
 
 // Compensated (Kahan) accumulation step: acc += x with running error c.

@@ -40,6 +40,8 @@ EbArgs eb_base_args(const EbGeom &g, void *ws, int N) {
   a.num_chunks = g.num_chunks;
   a.workers_per_block = g.workers_per_block;
   a.stage = g.stage;
+  a.use_tma = 0;
+  a.err = nullptr;
   CarryView cv = carry_view(ws, g.num_chunks, N);
   a.carry_rows = cv.rows;
   a.carry_vals = cv.vals;

@@ -36,6 +36,8 @@ struct EbArgs {
   int colgroups, log2_colgroups;  // pr kernels: column groups per worker
   int col_tile;
   int chunk, num_chunks, workers_per_block, stage;
+  int use_tma;          // sr kernels: stage the streams with bulk copies
+  int *err;             // device status word for bounded waits (may be null)
   int32_t *carry_rows;  // [num_chunks] head row of each chunk, -1 = none
   float *carry_vals;    // [num_chunks * N] head-row partials
   float *tail_vals;     // [num_chunks * N] partial of a last row that continues

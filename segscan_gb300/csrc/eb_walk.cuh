@@ -1,0 +1,405 @@
+// Element-balanced, sequential reduction: ebsr SpMM and the sequential
+// segment_coo family.
+//
+// Reference counterparts: csrspmm_rowcaching_nnzbalance_cg_kernel
+// (test-cg/include/spmm/spmm_cg.cuh:376-551) and segscan_sr_kernel /
+// segscan_sr_noshmem_kernel / segscan_sr_noshmem_lessatom_kernel /
+// segscan_sr_sorted_kernel (new-cg/include/segscan/segscan.cuh:357-815).
+//
+// A worker is a group of G lanes laid along N: lane l owns E = V*NV
+// consecutive columns, so one gathered B row is a single contiguous request
+// across the group.  A worker walks its chunk of nonzeros in order:
+//  * the chunk's column and value streams are staged in shared memory in
+//    tiles of S nonzeros by TMA bulk copies (cp.async.bulk completed on an
+//    mbarrier), double buffered so the next tile lands while this one is
+//    walked; misaligned streams fall back to coalesced loads;
+//  * the first row is found by a G-ary search of indptr (every lane probes
+//    one split point per round), and rows are then tracked from a window of
+//    indptr staged in shared memory - no per-nonzero search;
+//  * eight B rows are gathered ahead of the multiply-adds;
+//  * a row is flushed when the walk passes its end (eb_common.cuh: owner
+//    store, head/tail slots for the two rows that straddle the chunk,
+//    zeros for empty rows).
+// Every wait on an mbarrier is bounded; on expiry the kernel records
+// SS_ERR_TIMEOUT in the device flag a.err (ss_device_error) and skips the
+// chunk.  This header holds the kernel templates; eb_walk_*.cu instantiate
+// them per storage type and eb_walk.cu launches them.
+#pragma once
+#include "eb_common.cuh"
+#include "internal.h"
+
+namespace ss {
+
+constexpr int SR_U = 8;                       // B rows gathered ahead
+constexpr uint32_t SR_SPIN_LIMIT = 1u << 22;  // try_wait polls before giving up
+
+// Per-group shared memory: [bar0 bar1 | col[2][S] | val[2][S] | win[W]]
+struct SrLayout {
+  int S, W, vs;
+  int col_off, val_off, win_off, bytes;
+};
+
+__host__ __device__ inline SrLayout sr_layout(int S, int vs) {
+  SrLayout L;
+  L.S = S;
+  L.W = S + 8;
+  L.vs = vs;
+  int o = 16;  // two mbarriers
+  L.col_off = o;
+  o += 2 * S * 4;
+  L.val_off = o;
+  o += (2 * S * vs + 15) & ~15;
+  L.win_off = o;
+  o += L.W * 4;
+  L.bytes = (o + 15) & ~15;
+  return L;
+}
+
+struct Stage {
+  uint64_t *bar;  // [2]
+  int32_t *col;   // [2][S]
+  char *val;      // [2][S * vs]
+  int32_t *win;   // [W]
+  uint32_t phase[2];
+  bool tma[2];
+};
+
+// Starts loading nonzeros [sb, sb + n) into buffer b.
+template <typename T, bool SEG>
+__device__ __forceinline__ void stage_issue(const EbArgs &a, Stage &st, const SrLayout &L, int b, int sb, int n,
+                                            int lane, int G, unsigned mask, uint64_t strm) {
+  int32_t *dcol = st.col + b * L.S;
+  T *dval = reinterpret_cast<T *>(st.val + b * L.S * L.vs);
+  const int32_t *scol = SEG ? a.index : a.cols;
+  const T *sval = SEG ? nullptr : (const T *)a.vals;
+  __syncwarp(mask);  // every lane is done reading buffer b
+  st.tma[b] = a.use_tma && (n % 8) == 0;
+  if (st.tma[b]) {
+    if (lane == 0) {
+      fence_async_smem();
+      const uint32_t bytes = (uint32_t)n * 4u + (sval ? (uint32_t)n * (uint32_t)sizeof(T) : 0u);
+      mbar_expect_tx(st.bar + b, bytes);
+      bulk_g2s(dcol, scol + sb, (uint32_t)n * 4u, st.bar + b);
+      if (sval) bulk_g2s(dval, sval + sb, (uint32_t)n * (uint32_t)sizeof(T), st.bar + b);
+    }
+  } else {
+    for (int i = lane; i < n; i += G) {
+      dcol[i] = ld_idx(scol + sb + i, strm);
+      if (sval) dval[i] = sval[sb + i];
+    }
+  }
+}
+
+// Waits for buffer b; false when the bounded wait expired.
+__device__ __forceinline__ bool stage_wait(Stage &st, int b, unsigned mask, int *err) {
+  bool ok = true;
+  if (st.tma[b]) {
+    uint32_t it = 0;
+    while (!mbar_try_wait(st.bar + b, st.phase[b])) {
+      if (++it > SR_SPIN_LIMIT) {
+        if (err) atomicExch(err, (int)SS_ERR_TIMEOUT);
+        ok = false;
+        break;
+      }
+    }
+    st.phase[b] ^= 1u;
+  }
+  __syncwarp(mask);
+  return ok;
+}
+
+// First r in [0, M] with indptr[r] >= key, found by all G lanes of the
+// group: each round every lane probes one of G split points of [lo, hi].
+__device__ __forceinline__ int group_lower_bound(const int32_t *indptr, int M, int key, int lane, int G,
+                                                 unsigned mask) {
+  int lo = 0, hi = M;  // answer in [lo, hi]
+  const unsigned lanes_bits = G >= 32 ? 0xffffffffu : ((1u << G) - 1u);
+  const unsigned shift = (threadIdx.x & 31u) & ~(unsigned)(G - 1);
+  while (lo < hi) {
+    const long long span = (long long)(hi - lo);
+    const int probe = lo + (int)((span * (lane + 1)) / (G + 1));
+    const bool ge = __ldg(indptr + probe) >= key;
+    const unsigned hits = (__ballot_sync(mask, ge) >> shift) & lanes_bits;
+    const int first = hits ? __ffs(hits) - 1 : G;  // first lane whose probe is >= key
+    const int nhi = first < G ? __shfl_sync(mask, probe, first, G) : hi;
+    const int nlo = first > 0 ? __shfl_sync(mask, probe, first - 1, G) + 1 : lo;
+    lo = nlo;
+    hi = nhi;
+  }
+  return lo;
+}
+
+template <int V, int NV, bool KAHAN>
+__device__ __forceinline__ void add_row(float (&acc)[NV][V], float (&comp)[NV][V], float v,
+                                        const float (&b)[NV][V]) {
+  #pragma unroll
+  for (int j = 0; j < NV; j++)
+    #pragma unroll
+    for (int i = 0; i < V; i++) {
+      if (KAHAN) kahan_add(acc[j][i], comp[j][i], v * b[j][i]);
+      else acc[j][i] = fmaf(v, b[j][i], acc[j][i]);
+    }
+}
+
+// ---------------------------------------------------------------------
+// SpMM chunk walk
+// ---------------------------------------------------------------------
+template <typename T, typename TC, int V, int NV, bool KAHAN>
+__device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
+                                              const SrLayout &L, int col0, const bool (&act)[NV], uint64_t keep,
+                                              uint64_t strm) {
+  const T *__restrict__ B = (const T *)a.B;
+  const int G = a.team_lanes;
+  const bool ones = a.vals == nullptr;
+  ChunkInfo ci;
+  ci.cs = chunk * a.chunk;
+  ci.ce = min(ci.cs + a.chunk, a.nnz);
+  const int nst = (ci.ce - ci.cs + L.S - 1) / L.S;
+  stage_issue<T, false>(a, st, L, 0, ci.cs, min(L.S, ci.ce - ci.cs), lane, G, mask, strm);
+  if (nst > 1) stage_issue<T, false>(a, st, L, 1, ci.cs + L.S, min(L.S, ci.ce - ci.cs - L.S), lane, G, mask, strm);
+
+  // first row: lb = first row starting at or after cs
+  const int lb = group_lower_bound(a.indptr, a.M, ci.cs, lane, G, mask);
+  int win_base = lb;
+  auto win_fill = [&](int base) {
+    __syncwarp(mask);
+    win_base = base;
+    for (int i = lane; i < L.W; i += G) st.win[i] = __ldg(a.indptr + min(base + i, a.M));
+    __syncwarp(mask);
+  };
+  auto wget = [&](int r) -> int {
+    if (r - win_base >= L.W) win_fill(r);
+    return st.win[r - win_base];
+  };
+  win_fill(lb);
+  int cur;
+  ci.has_head = lb > 0 && wget(lb) > ci.cs;  // cs lies inside row lb - 1
+  if (ci.has_head) {
+    cur = lb - 1;
+  } else {
+    cur = lb;
+    // rows that start and end at cs are empty; this chunk owns them
+    while (cur < a.M - 1 && wget(cur + 1) <= ci.cs) {
+      if (!a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
+      cur++;
+    }
+  }
+  ci.r_first = cur;
+  ci.r_last = cur;
+  ci.prev_row = -1;
+  if (blockIdx.y == 0 && lane == 0) a.carry_rows[chunk] = ci.has_head ? cur : -1;
+  int next_start = wget(cur + 1);
+
+  int cnt = 0;
+  float acc[NV][V], comp[NV][V];
+  #pragma unroll
+  for (int j = 0; j < NV; j++)
+    #pragma unroll
+    for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
+
+  for (int s = 0; s < nst; s++) {
+    const int b = s & 1;
+    const int sb = ci.cs + s * L.S;
+    const int n = min(L.S, ci.ce - sb);
+    if (!stage_wait(st, b, mask, a.err)) return;
+    const int32_t *scol = st.col + b * L.S;
+    const T *sval = reinterpret_cast<const T *>(st.val + b * L.S * L.vs);
+    for (int q = 0; q < n; q += SR_U) {
+      float bv[SR_U][NV][V];
+      #pragma unroll
+      for (int u = 0; u < SR_U; u++) {
+        const int c = q + u < n ? scol[q + u] : -1;
+        const bool live = (unsigned)c < (unsigned)a.K;
+        #pragma unroll
+        for (int j = 0; j < NV; j++) {
+          if (live && act[j]) {
+            load_vec<T, V>(B + (int64_t)c * a.N + col0 + j * V, bv[u][j], keep);
+          } else {
+            #pragma unroll
+            for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+          }
+        }
+      }
+      #pragma unroll
+      for (int u = 0; u < SR_U; u++) {
+        if (q + u >= n) break;
+        const int p = sb + q + u;
+        if (p >= next_start) {  // the walk left row cur
+          flush_row<TC, V, NV>(a, ci, chunk, cur, acc, cnt, true, col0, act, strm);
+          int ns;
+          do {
+            cur++;
+            ns = wget(cur + 1);
+            if (ns <= p && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
+          } while (ns <= p && cur < a.M - 1);
+          next_start = ns;
+          cnt = 0;
+          #pragma unroll
+          for (int j = 0; j < NV; j++)
+            #pragma unroll
+            for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
+        }
+        const float v = ones ? 1.f : Elem<T>::to_f(sval[q + u]);
+        cnt++;
+        add_row<V, NV, KAHAN>(acc, comp, v, bv[u]);
+      }
+    }
+    if (s + 2 < nst)
+      stage_issue<T, false>(a, st, L, b, sb + 2 * L.S, min(L.S, ci.ce - sb - 2 * L.S), lane, G, mask, strm);
+  }
+  flush_row<TC, V, NV>(a, ci, chunk, cur, acc, cnt, next_start <= ci.ce, col0, act, strm);
+  if (!a.accumulate && ci.ce >= a.nnz) zero_rows<TC, V, NV>(a, cur + 1, a.M - 1, col0, act, strm);
+}
+
+// ---------------------------------------------------------------------
+// segment_coo chunk walk: segment ids come from the staged sorted index,
+// src rows are streamed in order
+// ---------------------------------------------------------------------
+template <typename T, int V, int NV, bool KAHAN>
+__device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
+                                             const SrLayout &L, int col0, const bool (&act)[NV], uint64_t strm) {
+  const T *__restrict__ src = (const T *)a.B;
+  const int G = a.team_lanes;
+  const bool is_max = a.reduce == SS_MAX;
+  const float ident = is_max ? -INFINITY : 0.f;
+  ChunkInfo ci;
+  ci.cs = chunk * a.chunk;
+  ci.ce = min(ci.cs + a.chunk, a.nnz);
+  const int nst = (ci.ce - ci.cs + L.S - 1) / L.S;
+  stage_issue<T, true>(a, st, L, 0, ci.cs, min(L.S, ci.ce - ci.cs), lane, G, mask, strm);
+  if (nst > 1) stage_issue<T, true>(a, st, L, 1, ci.cs + L.S, min(L.S, ci.ce - ci.cs - L.S), lane, G, mask, strm);
+  ci.r_first = __ldg(a.index + ci.cs);
+  ci.r_last = ci.r_first;
+  ci.prev_row = ci.cs > 0 ? __ldg(a.index + ci.cs - 1) : -1;
+  ci.has_head = ci.cs > 0 && ci.prev_row == ci.r_first;
+  if (blockIdx.y == 0 && lane == 0) a.carry_rows[chunk] = ci.has_head ? ci.r_first : -1;
+  if (!a.accumulate && !ci.has_head)
+    zero_rows<float, V, NV>(a, ci.prev_row + 1, ci.r_first - 1, col0, act, strm);
+
+  int cur = ci.r_first;
+  int cnt = 0;
+  float acc[NV][V], comp[NV][V];
+  #pragma unroll
+  for (int j = 0; j < NV; j++)
+    #pragma unroll
+    for (int i = 0; i < V; i++) { acc[j][i] = ident; comp[j][i] = 0.f; }
+
+  for (int s = 0; s < nst; s++) {
+    const int b = s & 1;
+    const int sb = ci.cs + s * L.S;
+    const int n = min(L.S, ci.ce - sb);
+    if (!stage_wait(st, b, mask, a.err)) return;
+    const int32_t *sidx = st.col + b * L.S;
+    for (int q = 0; q < n; q += SR_U) {
+      float bv[SR_U][NV][V];
+      #pragma unroll
+      for (int u = 0; u < SR_U; u++) {
+        const bool live = q + u < n;
+        #pragma unroll
+        for (int j = 0; j < NV; j++) {
+          if (live && act[j]) {
+            load_vec<T, V>(src + (int64_t)(sb + q + u) * a.N + col0 + j * V, bv[u][j], strm);
+          } else {
+            #pragma unroll
+            for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+          }
+        }
+      }
+      #pragma unroll
+      for (int u = 0; u < SR_U; u++) {
+        if (q + u >= n) break;
+        const int r = sidx[q + u];
+        if (r != cur) {
+          flush_row<float, V, NV>(a, ci, chunk, cur, acc, cnt, true, col0, act, strm);
+          if (!a.accumulate) zero_rows<float, V, NV>(a, cur + 1, r - 1, col0, act, strm);
+          cur = r;
+          cnt = 0;
+          #pragma unroll
+          for (int j = 0; j < NV; j++)
+            #pragma unroll
+            for (int i = 0; i < V; i++) { acc[j][i] = ident; comp[j][i] = 0.f; }
+        }
+        cnt++;
+        #pragma unroll
+        for (int j = 0; j < NV; j++)
+          #pragma unroll
+          for (int i = 0; i < V; i++) {
+            if (is_max) acc[j][i] = fmaxf(acc[j][i], bv[u][j][i]);
+            else if (KAHAN) kahan_add(acc[j][i], comp[j][i], bv[u][j][i]);
+            else acc[j][i] += bv[u][j][i];
+          }
+      }
+    }
+    if (s + 2 < nst)
+      stage_issue<T, true>(a, st, L, b, sb + 2 * L.S, min(L.S, ci.ce - sb - 2 * L.S), lane, G, mask, strm);
+  }
+  const bool complete = ci.ce >= a.nnz || __ldg(a.index + ci.ce) != cur;
+  flush_row<float, V, NV>(a, ci, chunk, cur, acc, cnt, complete, col0, act, strm);
+  if (!a.accumulate && ci.ce >= a.nnz) zero_rows<float, V, NV>(a, cur + 1, a.M - 1, col0, act, strm);
+}
+
+template <typename T, typename TC, int V, int NV, bool SEG>
+__global__ void __launch_bounds__(512) eb_sr_kernel(EbArgs a) {
+  extern __shared__ __align__(16) char smem_raw[];
+  const int tid = threadIdx.x;
+  const int G = a.team_lanes;
+  const int lane = tid & (G - 1);
+  const int wib = tid >> a.log2_team_lanes;
+  const unsigned wl = tid & 31;
+  const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
+  const SrLayout L = sr_layout(a.stage, SEG ? 0 : (int)sizeof(T));
+  char *g = smem_raw + (size_t)wib * L.bytes;
+  Stage st;
+  st.bar = reinterpret_cast<uint64_t *>(g);
+  st.col = reinterpret_cast<int32_t *>(g + L.col_off);
+  st.val = g + L.val_off;
+  st.win = reinterpret_cast<int32_t *>(g + L.win_off);
+  st.phase[0] = st.phase[1] = 0;
+  st.tma[0] = st.tma[1] = false;
+  if (lane == 0) {
+    mbar_init(st.bar, 1);
+    mbar_init(st.bar + 1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp(mask);
+  const int col0 = blockIdx.y * a.col_tile + lane * (V * NV);
+  bool act[NV];
+  #pragma unroll
+  for (int j = 0; j < NV; j++) act[j] = col0 + j * V < a.N;
+  const uint64_t keep = policy_keep(), strm = policy_stream();
+  const bool kahan = a.chunk > a.kahan;
+  const int stride = gridDim.x * a.workers_per_block;
+  for (int chunk = blockIdx.x * a.workers_per_block + wib; chunk < a.num_chunks; chunk += stride) {
+    if (SEG) {
+      if (kahan) sr_seg_chunk<T, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, strm);
+      else sr_seg_chunk<T, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, strm);
+    } else {
+      if (kahan) sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
+      else sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
+    }
+  }
+  // every issued stage was waited for: no bulk copy is in flight here
+}
+
+template <typename T, typename TC, bool SEG>
+inline void *sr_ptr(int V, int NV) {
+  if (NV == 1) {
+    if (V == 1) return (void *)eb_sr_kernel<T, TC, 1, 1, SEG>;
+    if (V == 2) return (void *)eb_sr_kernel<T, TC, 2, 1, SEG>;
+    if (V == 4) return (void *)eb_sr_kernel<T, TC, 4, 1, SEG>;
+    if constexpr (sizeof(T) == 2) if (V == 8) return (void *)eb_sr_kernel<T, TC, 8, 1, SEG>;
+  } else {
+    if (V == 1) return (void *)eb_sr_kernel<T, TC, 1, 2, SEG>;
+    if (V == 2) return (void *)eb_sr_kernel<T, TC, 2, 2, SEG>;
+    if (V == 4) return (void *)eb_sr_kernel<T, TC, 4, 2, SEG>;
+    if constexpr (sizeof(T) == 2) if (V == 8) return (void *)eb_sr_kernel<T, TC, 8, 2, SEG>;
+  }
+  return nullptr;
+}
+
+// Kernel tables, one translation unit per storage type (eb_walk_*.cu).
+void *sr_kernel_f32(int V, int NV, bool seg);
+void *sr_kernel_bf16(int V, int NV, bool seg, bool out_f32);
+void *sr_kernel_f16(int V, int NV, bool seg, bool out_f32);
+
+}  // namespace ss
