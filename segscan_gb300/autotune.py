@@ -62,8 +62,10 @@ def candidates(N: int) -> list[tuple[str, dict]]:
         c.append(("rbpr", dict(group_factor=gf, tile_factor=tf, block_denom=denom)))
     lanes_gf = max(0, min(5, int(math.log2(max(1, N // 4)))))
     for gf in sorted({lanes_gf, max(0, lanes_gf - 1)}):
-        for tnz in (2, 4, 8, 16, 32):
-            c.append(("ebsr", dict(group_factor=gf, coarsen_factor=4, thread_nz=tnz, block_denom=1)))
+        for tnz in (2, 4, 8, 16, 32, 64):
+            for tpb in (128, 256, 512):
+                c.append(("ebsr", dict(group_factor=gf, coarsen_factor=4, thread_nz=tnz, block_denom=1,
+                                       thread_per_block=tpb)))
     for cf, tf in ((4, 5), (4, 6), (2, 5)):
         c.append(("rbsr", dict(coarsen_factor=cf, tile_factor=tf)))
     return c
