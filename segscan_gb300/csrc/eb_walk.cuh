@@ -16,7 +16,8 @@
 //  * the first row is found by a G-ary search of indptr (every lane probes
 //    one split point per round), and rows are then tracked from a window of
 //    indptr staged in shared memory - no per-nonzero search;
-//  * eight B rows are gathered ahead of the multiply-adds;
+//  * four B rows are gathered ahead of the multiply-adds, with registers
+//    capped at 64 so that 32+ warps per SM keep enough gathers in flight;
 //  * a row is flushed when the walk passes its end (eb_common.cuh: owner
 //    store, head/tail slots for the two rows that straddle the chunk,
 //    zeros for empty rows).
@@ -30,7 +31,7 @@
 
 namespace ss {
 
-constexpr int SR_U = 8;                       // B rows gathered ahead
+constexpr int SR_U = 4;                       // B rows gathered ahead
 constexpr uint32_t SR_SPIN_LIMIT = 1u << 22;  // try_wait polls before giving up
 
 // Per-group shared memory: [bar0 bar1 | col[2][S] | val[2][S] | win[W]]
@@ -56,12 +57,12 @@ __host__ __device__ inline SrLayout sr_layout(int S, int vs) {
 }
 
 struct Stage {
-  uint64_t *bar;  // [2]
-  int32_t *col;   // [2][S]
-  char *val;      // [2][S * vs]
-  int32_t *win;   // [W]
-  uint32_t phase[2];
-  bool tma[2];
+  uint64_t *bar;    // [2]
+  int32_t *col;     // [2][S]
+  char *val;        // [2][S * vs]
+  int32_t *win;     // [W]
+  uint32_t phases;  // bit b: parity to wait for on bar[b]
+  uint32_t tma;     // bit b: buffer b was filled by a bulk copy
 };
 
 // Starts loading nonzeros [sb, sb + n) into buffer b.
@@ -73,8 +74,9 @@ __device__ __forceinline__ void stage_issue(const EbArgs &a, Stage &st, const Sr
   const int32_t *scol = SEG ? a.index : a.cols;
   const T *sval = SEG ? nullptr : (const T *)a.vals;
   __syncwarp(mask);  // every lane is done reading buffer b
-  st.tma[b] = a.use_tma && (n % 8) == 0;
-  if (st.tma[b]) {
+  const bool tma = a.use_tma && (n % 8) == 0;
+  st.tma = tma ? (st.tma | (1u << b)) : (st.tma & ~(1u << b));
+  if (tma) {
     if (lane == 0) {
       fence_async_smem();
       const uint32_t bytes = (uint32_t)n * 4u + (sval ? (uint32_t)n * (uint32_t)sizeof(T) : 0u);
@@ -93,16 +95,16 @@ __device__ __forceinline__ void stage_issue(const EbArgs &a, Stage &st, const Sr
 // Waits for buffer b; false when the bounded wait expired.
 __device__ __forceinline__ bool stage_wait(Stage &st, int b, unsigned mask, int *err) {
   bool ok = true;
-  if (st.tma[b]) {
+  if (st.tma & (1u << b)) {
     uint32_t it = 0;
-    while (!mbar_try_wait(st.bar + b, st.phase[b])) {
+    while (!mbar_try_wait(st.bar + b, (st.phases >> b) & 1u)) {
       if (++it > SR_SPIN_LIMIT) {
         if (err) atomicExch(err, (int)SS_ERR_TIMEOUT);
         ok = false;
         break;
       }
     }
-    st.phase[b] ^= 1u;
+    st.phases ^= 1u << b;
   }
   __syncwarp(mask);
   return ok;
@@ -339,7 +341,7 @@ __device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lan
 }
 
 template <typename T, typename TC, int V, int NV, bool SEG>
-__global__ void __launch_bounds__(512) eb_sr_kernel(EbArgs a) {
+__global__ void __launch_bounds__(512, 2) eb_sr_kernel(EbArgs a) {
   extern __shared__ __align__(16) char smem_raw[];
   const int tid = threadIdx.x;
   const int G = a.team_lanes;
@@ -354,8 +356,8 @@ __global__ void __launch_bounds__(512) eb_sr_kernel(EbArgs a) {
   st.col = reinterpret_cast<int32_t *>(g + L.col_off);
   st.val = g + L.val_off;
   st.win = reinterpret_cast<int32_t *>(g + L.win_off);
-  st.phase[0] = st.phase[1] = 0;
-  st.tma[0] = st.tma[1] = false;
+  st.phases = 0;
+  st.tma = 0;
   if (lane == 0) {
     mbar_init(st.bar, 1);
     mbar_init(st.bar + 1, 1);
