@@ -37,19 +37,23 @@ constexpr uint32_t SR_SPIN_LIMIT = 1u << 22;  // try_wait polls before giving up
 // Per-group shared memory: [bar0 bar1 | col[2][S] | val[2][S] | win[W]]
 struct SrLayout {
   int S, W, vs;
-  int col_off, val_off, win_off, bytes;
+  int col_off, val_off, info_off, win_off, bytes;
 };
 
+// Per-group shared memory: [bar0 bar1 | col[2][S] | val[2][S] | info[2][S] |
+// win[W]].  info holds, per staged nonzero, its row and an end-of-row bit.
 __host__ __device__ inline SrLayout sr_layout(int S, int vs) {
   SrLayout L;
   L.S = S;
-  L.W = S + 8;
+  L.W = 2 * S + 8;
   L.vs = vs;
   int o = 16;  // two mbarriers
   L.col_off = o;
   o += 2 * S * 4;
   L.val_off = o;
   o += (2 * S * vs + 15) & ~15;
+  L.info_off = o;
+  o += 2 * S * 4;
   L.win_off = o;
   o += L.W * 4;
   L.bytes = (o + 15) & ~15;
@@ -60,6 +64,7 @@ struct Stage {
   uint64_t *bar;    // [2]
   int32_t *col;     // [2][S]
   char *val;        // [2][S * vs]
+  int32_t *info;    // [2][S]
   int32_t *win;     // [W]
   uint32_t phases;  // bit b: parity to wait for on bar[b]
   uint32_t tma;     // bit b: buffer b was filled by a bulk copy
@@ -145,7 +150,35 @@ __device__ __forceinline__ void add_row(float (&acc)[NV][V], float (&comp)[NV][V
 
 // ---------------------------------------------------------------------
 // SpMM chunk walk
+//
+// State carried from tile to tile: cur = row of the latest nonzero (or the
+// chunk's first row), acc = partial of cur that is not yet written (open).
+// Fast tile: the lanes first label every staged nonzero with its row and an
+// end-of-row bit (binary search in the indptr window, in parallel) and zero
+// the empty rows that follow a row end; the walk then only gathers,
+// multiplies, and stores on the end bits.  A tile whose rows do not fit the
+// window (long runs of empty rows) is walked element by element instead.
 // ---------------------------------------------------------------------
+template <typename TC, int V, int NV>
+__device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)[NV][V], int col0,
+                                          const bool (&act)[NV], uint64_t pol) {
+  TC *C = (TC *)a.C;
+  #pragma unroll
+  for (int j = 0; j < NV; j++) {
+    if (!act[j]) continue;
+    TC *dst = C + (int64_t)row * a.N + col0 + j * V;
+    if (a.accumulate) {
+      float prev[V], out[V];
+      load_out<TC, V>(dst, prev);
+      #pragma unroll
+      for (int i = 0; i < V; i++) out[i] = acc[j][i] + prev[i];
+      store_vec<TC, V>(dst, out, pol);
+    } else {
+      store_vec<TC, V>(dst, acc[j], pol);
+    }
+  }
+}
+
 template <typename T, typename TC, int V, int NV, bool KAHAN>
 __device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
                                               const SrLayout &L, int col0, const bool (&act)[NV], uint64_t keep,
@@ -170,7 +203,7 @@ __device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int la
     __syncwarp(mask);
   };
   auto wget = [&](int r) -> int {
-    if (r - win_base >= L.W) win_fill(r);
+    if (r - win_base >= L.W || r < win_base) win_fill(r);
     return st.win[r - win_base];
   };
   win_fill(lb);
@@ -190,44 +223,139 @@ __device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int la
   ci.r_last = cur;
   ci.prev_row = -1;
   if (blockIdx.y == 0 && lane == 0) a.carry_rows[chunk] = ci.has_head ? cur : -1;
-  int next_start = wget(cur + 1);
+  const int head = ci.has_head ? cur : -1;
 
-  int cnt = 0;
+  bool open = false;
   float acc[NV][V], comp[NV][V];
   #pragma unroll
   for (int j = 0; j < NV; j++)
     #pragma unroll
     for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
 
+  // writes acc for row r (head slot, owner store) and clears it
+  auto flush_done = [&](int r) {
+    if (r == head) {
+      #pragma unroll
+      for (int j = 0; j < NV; j++)
+        if (act[j]) store_vec<float, V>(a.carry_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], strm);
+    } else if ((unsigned)r < (unsigned)a.M) {
+      store_out<TC, V, NV>(a, r, acc, col0, act, strm);
+    }
+    #pragma unroll
+    for (int j = 0; j < NV; j++)
+      #pragma unroll
+      for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
+  };
+
   for (int s = 0; s < nst; s++) {
     const int b = s & 1;
     const int sb = ci.cs + s * L.S;
     const int n = min(L.S, ci.ce - sb);
+    const int last = sb + n - 1;
     if (!stage_wait(st, b, mask, a.err)) return;
     const int32_t *scol = st.col + b * L.S;
     const T *sval = reinterpret_cast<const T *>(st.val + b * L.S * L.vs);
-    for (int q = 0; q < n; q += SR_U) {
-      float bv[SR_U][NV][V];
-      #pragma unroll
-      for (int u = 0; u < SR_U; u++) {
-        const int c = q + u < n ? scol[q + u] : -1;
-        const bool live = (unsigned)c < (unsigned)a.K;
+    int32_t *sinfo = st.info + b * L.S;
+
+    // the window must hold the starts of every row this tile touches and of
+    // the row after the last one
+    if (cur < win_base || st.win[L.W - 1] <= last) win_fill(cur);
+    const bool fast = st.win[L.W - 1] > last || win_base + L.W - 1 >= a.M;
+
+    if (fast) {
+      // ---- label the tile's nonzeros with row | end-of-row bit; empty rows
+      // starting where a row's first nonzero sits are zeroed by the whole
+      // group (each lane owns one column slice)
+      const int c0 = cur - win_base;
+      const int rounds = (n + G - 1) / G;
+      for (int k = 0; k < rounds; k++) {
+        const int e = lane + k * G;
+        int zlo = 0, zhi = -1;
+        if (e < n) {
+          const int p = sb + e;
+          int lo = c0 + 1, hi = L.W - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (st.win[mid] <= p) lo = mid + 1; else hi = mid;
+          }
+          const int rr = lo - 1;  // window slot of p's row
+          const bool end = st.win[rr + 1] == p + 1;
+          sinfo[e] = (win_base + rr) | (end ? (int)0x80000000 : 0);
+          if (st.win[rr] == p && p != ci.cs) {  // p opens row rr: empties before it start at p too
+            int q = rr - 1;
+            while (q > c0 && st.win[q] == p) q--;
+            zlo = win_base + q + 1;
+            zhi = win_base + rr - 1;
+          }
+        }
+        unsigned todo = __ballot_sync(mask, zlo <= zhi);
+        while (todo) {
+          const int src = __ffs(todo) - 1;
+          const int lo_r = __shfl_sync(mask, zlo, src);
+          const int hi_r = __shfl_sync(mask, zhi, src);
+          if (!a.accumulate) zero_rows<TC, V, NV>(a, lo_r, hi_r, col0, act, strm);
+          todo &= todo - 1;
+        }
+      }
+      __syncwarp(mask);
+      // ---- walk: gather, multiply, store at row ends
+      for (int q = 0; q < n; q += SR_U) {
+        float bv[SR_U][NV][V];
         #pragma unroll
-        for (int j = 0; j < NV; j++) {
-          if (live && act[j]) {
-            load_vec<T, V>(B + (int64_t)c * a.N + col0 + j * V, bv[u][j], keep);
-          } else {
-            #pragma unroll
-            for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+        for (int u = 0; u < SR_U; u++) {
+          const int c = q + u < n ? scol[q + u] : -1;
+          const bool live = (unsigned)c < (unsigned)a.K;
+          #pragma unroll
+          for (int j = 0; j < NV; j++) {
+            if (live && act[j]) {
+              load_vec<T, V>(B + (int64_t)c * a.N + col0 + j * V, bv[u][j], keep);
+            } else {
+              #pragma unroll
+              for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+            }
+          }
+        }
+        #pragma unroll
+        for (int u = 0; u < SR_U; u++) {
+          if (q + u >= n) break;
+          const int info = sinfo[q + u];
+          const float v = ones ? 1.f : Elem<T>::to_f(sval[q + u]);
+          add_row<V, NV, KAHAN>(acc, comp, v, bv[u]);
+          cur = info & 0x7fffffff;
+          open = true;
+          if (info < 0) {
+            flush_done(cur);
+            open = false;
           }
         }
       }
-      #pragma unroll
-      for (int u = 0; u < SR_U; u++) {
-        if (q + u >= n) break;
-        const int p = sb + q + u;
+    } else {
+      // ---- element by element (tiles crossing long runs of empty rows)
+      int next_start = wget(cur + 1);
+      if (!open) {
+        // the previous row ended at sb: move to the row of the tile's first
+        // nonzero, zeroing the empty rows on the way
+        while (cur < a.M - 1 && next_start <= sb) {
+          cur++;
+          next_start = wget(cur + 1);
+          if (next_start <= sb && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
+        }
+      }
+      for (int q = 0; q < n; q++) {
+        const int p = sb + q;
+        const int c = scol[q];
+        float bq[NV][V];
+        #pragma unroll
+        for (int j = 0; j < NV; j++) {
+          if ((unsigned)c < (unsigned)a.K && act[j]) {
+            load_vec<T, V>(B + (int64_t)c * a.N + col0 + j * V, bq[j], keep);
+          } else {
+            #pragma unroll
+            for (int i = 0; i < V; i++) bq[j][i] = 0.f;
+          }
+        }
         if (p >= next_start) {  // the walk left row cur
-          flush_row<TC, V, NV>(a, ci, chunk, cur, acc, cnt, true, col0, act, strm);
+          if (open) flush_done(cur);
           int ns;
           do {
             cur++;
@@ -235,21 +363,34 @@ __device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int la
             if (ns <= p && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
           } while (ns <= p && cur < a.M - 1);
           next_start = ns;
-          cnt = 0;
-          #pragma unroll
-          for (int j = 0; j < NV; j++)
-            #pragma unroll
-            for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
         }
-        const float v = ones ? 1.f : Elem<T>::to_f(sval[q + u]);
-        cnt++;
-        add_row<V, NV, KAHAN>(acc, comp, v, bv[u]);
+        const float v = ones ? 1.f : Elem<T>::to_f(sval[q]);
+        add_row<V, NV, KAHAN>(acc, comp, v, bq);
+        open = true;
+      }
+      // close a row that ends exactly at the tile end; the next tile zeroes
+      // any empty rows that follow it
+      if (next_start == last + 1) {
+        flush_done(cur);
+        open = false;
       }
     }
+    __syncwarp(mask);
     if (s + 2 < nst)
       stage_issue<T, false>(a, st, L, b, sb + 2 * L.S, min(L.S, ci.ce - sb - 2 * L.S), lane, G, mask, strm);
   }
-  flush_row<TC, V, NV>(a, ci, chunk, cur, acc, cnt, next_start <= ci.ce, col0, act, strm);
+  // the last row continues past the chunk: head slot or tail slot
+  if (open) {
+    if (cur == head) {
+      #pragma unroll
+      for (int j = 0; j < NV; j++)
+        if (act[j]) store_vec<float, V>(a.carry_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], strm);
+    } else {
+      #pragma unroll
+      for (int j = 0; j < NV; j++)
+        if (act[j]) store_vec<float, V>(a.tail_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], strm);
+    }
+  }
   if (!a.accumulate && ci.ce >= a.nnz) zero_rows<TC, V, NV>(a, cur + 1, a.M - 1, col0, act, strm);
 }
 
@@ -355,6 +496,7 @@ __global__ void __launch_bounds__(512, 2) eb_sr_kernel(EbArgs a) {
   st.bar = reinterpret_cast<uint64_t *>(g);
   st.col = reinterpret_cast<int32_t *>(g + L.col_off);
   st.val = g + L.val_off;
+  st.info = reinterpret_cast<int32_t *>(g + L.info_off);
   st.win = reinterpret_cast<int32_t *>(g + L.win_off);
   st.phases = 0;
   st.tma = 0;
