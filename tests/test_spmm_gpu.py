@@ -215,3 +215,42 @@ def test_validate(cuda):
     bad = A.indices.clone()
     bad[3] = 1000
     assert api.validate(api.CsrMatrix(A.nrow, A.ncol, A.indptr, bad, A.values)) & 8
+
+
+def empty_runs_matrix(seed=5, M=6000, K=3000):
+    """Short rows separated by runs of up to 400 empty rows (longer than any
+    shared-memory row window), plus long rows, so chunk and tile boundaries
+    land inside, before and after empty runs."""
+    rng = np.random.default_rng(seed)
+    lengths = np.zeros(M, np.int64)
+    r = 0
+    while r < M:
+        run = int(rng.integers(0, 400)) if rng.random() < 0.3 else 0
+        r += run
+        if r >= M:
+            break
+        lengths[r] = int(rng.integers(1, 9)) if rng.random() < 0.95 else int(rng.integers(200, 1500))
+        r += 1
+    return synth.csr_from_lengths(M, K, lengths, rng)
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+@pytest.mark.parametrize("accumulate", [False, True])
+def test_empty_row_runs(cuda, strategy, accumulate):
+    from segscan_gb300 import api
+    csr = empty_runs_matrix()
+    N = 16
+    B = synth.dense(csr.ncol, N, seed=6)
+    C0 = synth.dense(csr.nrow, N, seed=7)
+    C64, absC = oracle64(csr, B)
+    A = dev_csr(csr)
+    sweeps = {"ebsr": [dict(group_factor=2, thread_nz=t) for t in (1, 2, 8, 16, 32, 64)],
+              "ebpr": [dict(group_factor=5, tile_factor=5, block_denom=d) for d in (1, 16, 256)],
+              "rbpr": [dict(group_factor=3, tile_factor=3)], "rbsr": [dict(coarsen_factor=4, tile_factor=4)]}
+    for kw in sweeps[strategy]:
+        out = torch.from_numpy(C0.copy()).cuda() if accumulate else torch.full((csr.nrow, N), 9.0, device="cuda")
+        spmm(A, torch.from_numpy(B).cuda(), strategy, knobs=api.make_knobs(strategy, N, **kw), out=out,
+             accumulate=accumulate)
+        ref = C64 + C0 if accumulate else C64
+        check_close(out.cpu().numpy(), ref, absC + (np.abs(C0) if accumulate else 0), 1e-5, None,
+                    f"{strategy} {kw} acc={accumulate}")
