@@ -217,7 +217,7 @@ def test_validate(cuda):
     assert api.validate(api.CsrMatrix(A.nrow, A.ncol, A.indptr, bad, A.values)) & 8
 
 
-def empty_runs_matrix(seed=5, M=6000, K=3000):
+def empty_runs_matrix(seed=5, M=20000, K=3000):
     """Short rows separated by runs of up to 400 empty rows (longer than any
     shared-memory row window), plus long rows, so chunk and tile boundaries
     land inside, before and after empty runs."""
@@ -225,7 +225,7 @@ def empty_runs_matrix(seed=5, M=6000, K=3000):
     lengths = np.zeros(M, np.int64)
     r = 0
     while r < M:
-        run = int(rng.integers(0, 400)) if rng.random() < 0.3 else 0
+        run = int(rng.integers(0, 400)) if rng.random() < 0.08 else 0
         r += run
         if r >= M:
             break
