@@ -16,6 +16,7 @@
 //  * a coarsen factor that is not a power of two is rounded down and the
 //    column grid recomputed (the reference falls back to CoarsenFactor 1 but
 //    keeps the grid sized for the larger factor, dropping columns).
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -36,6 +37,26 @@ ss_status fail(ss_status st, const char *fmt, ...) {
 
 ss_status cuda_fail(cudaError_t err, const char *what) {
   return fail(SS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
+}
+
+// L2 budget for the gathered operand; 0 = half of the device's L2.
+static std::atomic<long long> g_keep_bytes{0};
+
+float l2_keep_fraction(size_t bytes) {
+  long long budget = g_keep_bytes.load(std::memory_order_relaxed);
+  if (budget <= 0) {
+    static int l2 = -1;
+    if (l2 < 0) {
+      int dev = 0, v = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) != cudaSuccess)
+        v = 64 << 20;
+      l2 = v;
+    }
+    budget = l2 / 2;
+  }
+  if (bytes == 0 || (long long)bytes <= budget) return 1.0f;
+  float f = (float)((double)budget / (double)bytes);
+  return f < 0.01f ? 0.01f : f;
 }
 
 // Largest power-of-two vector (<= 16 bytes, <= max_elems) dividing N.
@@ -296,6 +317,12 @@ const char *ss_status_string(int status) {
 }
 
 const char *ss_last_error(void) { return g_last_error; }
+
+ss_status ss_set_l2_keep_bytes(long long bytes) {
+  if (bytes < 0) return fail(SS_ERR_INVALID_ARG, "negative L2 budget");
+  g_keep_bytes.store(bytes, std::memory_order_relaxed);
+  return SS_OK;
+}
 
 ss_status ss_default_knobs(int strategy, int N, ss_knobs *out) {
   if (!out) return fail(SS_ERR_INVALID_ARG, "out is null");

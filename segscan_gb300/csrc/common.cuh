@@ -33,15 +33,12 @@ template <> struct Elem<__half> {
 // (evict_last).  The A streams and C are touched once: evict first so they
 // do not push B out of L2.
 // ------------------------------------------------------------------
-#ifndef SS_KEEP_FRACTION
-#define SS_KEEP_FRACTION 1.0
-#endif
-#define SS_STR2(x) #x
-#define SS_STR(x) SS_STR2(x)
-__device__ __forceinline__ uint64_t policy_keep() {
+// `frac` of B's lines (a fixed subset by address) get evict_last, the rest
+// evict_first: when B is larger than L2, keeping a subset that fits gives
+// that subset hits instead of letting every line thrash.
+__device__ __forceinline__ uint64_t policy_keep(float frac) {
   uint64_t p;
-  asm("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, " SS_STR(SS_KEEP_FRACTION) ";"
-      : "=l"(p));
+  asm("createpolicy.fractional.L2::evict_last.L2::evict_first.b64 %0, %1;" : "=l"(p) : "f"(frac));
   return p;
 }
 __device__ __forceinline__ uint64_t policy_stream() {

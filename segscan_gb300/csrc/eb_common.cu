@@ -42,6 +42,7 @@ EbArgs eb_base_args(const EbGeom &g, void *ws, int N) {
   a.stage = g.stage;
   a.use_tma = 0;
   a.err = nullptr;
+  a.keep_frac = 1.0f;
   CarryView cv = carry_view(ws, g.num_chunks, N);
   a.carry_rows = cv.rows;
   a.carry_vals = cv.vals;

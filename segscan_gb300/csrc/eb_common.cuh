@@ -38,6 +38,7 @@ struct EbArgs {
   int chunk, num_chunks, workers_per_block, stage;
   int use_tma;          // sr kernels: stage the streams with bulk copies
   int *err;             // device status word for bounded waits (may be null)
+  float keep_frac;      // fraction of B's lines kept in L2 (evict_last)
   int32_t *carry_rows;  // [num_chunks] head row of each chunk, -1 = none
   float *carry_vals;    // [num_chunks * N] head-row partials
   float *tail_vals;     // [num_chunks * N] partial of a last row that continues

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(1024) eb_pr_kernel(EbArgs a) {
   const unsigned mask = tile >= 32 ? 0xffffffffu : (((1u << tile) - 1u) << (wl & ~(unsigned)(tile - 1)));
   const int col0 = blockIdx.y * a.col_tile + cg * V;
   bool act[1] = {col0 < a.N};
-  const uint64_t keep = policy_keep(), strm = policy_stream();
+  const uint64_t keep = policy_keep(a.keep_frac), strm = policy_stream();
   const bool is_max = SEG && a.reduce == SS_MAX;
   const float ident = is_max ? -INFINITY : 0.f;
   const int stride = gridDim.x * a.workers_per_block;
@@ -151,6 +151,7 @@ ss_status launch_ebpr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
   a.M = c.M; a.K = c.K; a.nnz = c.nnz;
   a.indptr = c.indptr; a.cols = c.indices; a.index = nullptr; a.vals = c.vals; a.B = c.B; a.C = c.C;
   a.accumulate = c.accumulate; a.reduce = SS_SUM; a.kahan = c.kahan_threshold;
+  a.keep_frac = l2_keep_fraction((size_t)c.K * c.N * dtype_size(c.val_dtype));
   void *fn;
   if (c.val_dtype == SS_F32) fn = pr_ptr<float, float, false>(g.cs.V);
   else if (c.val_dtype == SS_BF16)

@@ -63,6 +63,7 @@ ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
   a.M = c.M; a.K = c.K; a.nnz = c.nnz;
   a.indptr = c.indptr; a.cols = c.indices; a.index = nullptr; a.vals = c.vals; a.B = c.B; a.C = c.C;
   a.accumulate = c.accumulate; a.reduce = SS_SUM; a.kahan = c.kahan_threshold;
+  a.keep_frac = l2_keep_fraction((size_t)c.K * c.N * dtype_size(c.val_dtype));
   a.use_tma = aligned16(c.indices) && (c.vals == nullptr || aligned16(c.vals)) && (g.chunk % 8) == 0;
   a.err = walk_error_ptr();
   void *fn = nullptr;

@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(512, 2) eb_sr_kernel(EbArgs a) {
   bool act[NV];
   #pragma unroll
   for (int j = 0; j < NV; j++) act[j] = col0 + j * V < a.N;
-  const uint64_t keep = policy_keep(), strm = policy_stream();
+  const uint64_t keep = policy_keep(a.keep_frac), strm = policy_stream();
   const bool kahan = a.chunk > a.kahan;
   const int stride = gridDim.x * a.workers_per_block;
   for (int chunk = blockIdx.x * a.workers_per_block + wib; chunk < a.num_chunks; chunk += stride) {

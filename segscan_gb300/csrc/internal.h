@@ -94,6 +94,10 @@ CarryView carry_view(void *ws, int num_chunks, int N);
 ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *C, int c_dtype,
                        int reduce, int accumulate, const int32_t *index, int nnz, cudaStream_t s);
 
+// Fraction of a gathered operand of `bytes` to mark evict_last: all of it
+// when it fits the L2 budget, else the budget's share (abi.cu).
+float l2_keep_fraction(size_t bytes);
+
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 inline int floor_pow2(int x) {
   int p = 1;

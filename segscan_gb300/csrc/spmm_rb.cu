@@ -23,6 +23,7 @@ struct RbArgs {
   int slots, log2_slots;   // nonzero slots per team (1 for rbsr)
   int team_threads, log2_team;
   int teams_per_block;
+  float keep_frac;  // fraction of B's lines kept in L2 (evict_last)
 };
 
 template <int V, int NV> struct Acc {
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(1024) rbsr_kernel(RbArgs a) {
   bool act[NV];
   #pragma unroll
   for (int j = 0; j < NV; j++) act[j] = col0 + j * V < a.N;
-  const uint64_t keep = policy_keep(), strm = policy_stream();
+  const uint64_t keep = policy_keep(a.keep_frac), strm = policy_stream();
   const int stride = gridDim.x * a.teams_per_block;
   for (int row = blockIdx.x * a.teams_per_block + team; row < a.M; row += stride) {
     int s, e;
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(1024) rbpr_kernel(RbArgs a) {
   bool act[NV];
   #pragma unroll
   for (int j = 0; j < NV; j++) act[j] = col0 + j * V < a.N;
-  const uint64_t keep = policy_keep(), strm = policy_stream();
+  const uint64_t keep = policy_keep(a.keep_frac), strm = policy_stream();
   const int stride = gridDim.x * a.teams_per_block;
   // warps a team spans; 0 when the team fits in one warp (no shared memory then)
   const int warps_in_team = a.team_threads > 32 ? a.team_threads >> 5 : 0;
@@ -274,6 +275,7 @@ static RbArgs make_args(const SpmmCall &c, const RbGeom &g) {
   a.slots = g.slots; a.log2_slots = ilog2(g.slots);
   a.team_threads = g.team_threads; a.log2_team = ilog2(g.team_threads);
   a.teams_per_block = g.teams_per_block;
+  a.keep_frac = l2_keep_fraction((size_t)c.K * c.N * dtype_size(c.val_dtype));
   return a;
 }
 
