@@ -122,7 +122,7 @@ ss_status ss_device_error(int *status, int clear);
 /* L2 budget (bytes) for the gathered dense operand B: when B is larger,
  * only a fixed address subset of that size is marked evict_last and the
  * rest evict_first, so the kept subset stays resident.  0 (the default)
- * uses half of the device's L2.  Process-wide.  No counterpart in the
+ * marks all of B evict_last.  Process-wide.  No counterpart in the
  * reference. */
 ss_status ss_set_l2_keep_bytes(long long bytes);
 /* Knob tuple the reference's README reports as best static choice for a

@@ -39,22 +39,13 @@ ss_status cuda_fail(cudaError_t err, const char *what) {
   return fail(SS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
 }
 
-// L2 budget for the gathered operand; 0 = half of the device's L2.
+// L2 budget for the gathered operand; 0 = no budget (keep all of it, the
+// measured best on the power-law SpMM at N = 16, 64, 128).
 static std::atomic<long long> g_keep_bytes{0};
 
 float l2_keep_fraction(size_t bytes) {
-  long long budget = g_keep_bytes.load(std::memory_order_relaxed);
-  if (budget <= 0) {
-    static int l2 = -1;
-    if (l2 < 0) {
-      int dev = 0, v = 0;
-      if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) != cudaSuccess)
-        v = 64 << 20;
-      l2 = v;
-    }
-    budget = l2 / 2;
-  }
-  if (bytes == 0 || (long long)bytes <= budget) return 1.0f;
+  const long long budget = g_keep_bytes.load(std::memory_order_relaxed);
+  if (budget <= 0 || bytes == 0 || (long long)bytes <= budget) return 1.0f;
   float f = (float)((double)budget / (double)bytes);
   return f < 0.01f ? 0.01f : f;
 }
