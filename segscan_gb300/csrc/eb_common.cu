@@ -65,6 +65,9 @@ __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restr
                                                           const float *__restrict__ tails, int num_chunks,
                                                           int N, int M, TC *C, int reduce, int accumulate,
                                                           const int32_t *__restrict__ index, int nnz) {
+  // launched as a programmatic dependent of the walk kernel: wait until the
+  // walk's writes (head/tail slots, owner rows) are complete and visible
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += warps) {
@@ -105,18 +108,28 @@ ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *
   if (num_chunks <= 1 || N == 0 || M == 0) return SS_OK;  // chunk 0 never carries
   const int threads = 256;
   const int blocks = std::max(1, std::min((num_chunks + 7) / 8, 152 * 32));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e;
   if (c_dtype == SS_F32)
-    carry_fixup_kernel<float><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, cv.tails, num_chunks, N, M,
-                                                          (float *)C, reduce, accumulate, index, nnz);
+    e = cudaLaunchKernelEx(&cfg, carry_fixup_kernel<float>, (const int32_t *)cv.rows, (const float *)cv.vals,
+                           (const float *)cv.tails, num_chunks, N, M, (float *)C, reduce, accumulate, index, nnz);
   else if (c_dtype == SS_BF16)
-    carry_fixup_kernel<__nv_bfloat16><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, cv.tails, num_chunks, N,
-                                                                  M, (__nv_bfloat16 *)C, reduce, accumulate,
-                                                                  index, nnz);
+    e = cudaLaunchKernelEx(&cfg, carry_fixup_kernel<__nv_bfloat16>, (const int32_t *)cv.rows, (const float *)cv.vals,
+                           (const float *)cv.tails, num_chunks, N, M, (__nv_bfloat16 *)C, reduce, accumulate, index,
+                           nnz);
   else
-    carry_fixup_kernel<__half><<<blocks, threads, 0, s>>>(cv.rows, cv.vals, cv.tails, num_chunks, N, M,
-                                                           (__half *)C, reduce, accumulate, index, nnz);
-  cudaError_t err = cudaGetLastError();
-  if (err != cudaSuccess) return cuda_fail(err, "carry fix-up launch");
+    e = cudaLaunchKernelEx(&cfg, carry_fixup_kernel<__half>, (const int32_t *)cv.rows, (const float *)cv.vals,
+                           (const float *)cv.tails, num_chunks, N, M, (__half *)C, reduce, accumulate, index, nnz);
+  if (e != cudaSuccess) return cuda_fail(e, "carry fix-up launch");
   return SS_OK;
 }
 
