@@ -303,7 +303,7 @@ def segment_coo_sorted_sr(src, index, nnz, N, dst, *, CoarsenFactor, ThreadNz, D
     of ThreadNz consecutive elements; DtileNum x BlockDimY workers per block."""
     gf = max(0, min(5, int(DtileSize).bit_length() - 1))
     G = 1 << gf
-    tpb = max(G, min(1024, G * int(DtileNum) * int(BlockDimY)))
+    tpb = max(G, min(512, G * int(DtileNum) * int(BlockDimY)))
     tpb -= tpb % G
     _ref_segment("sr", src, index, nnz, N, dst, group_factor=gf, thread_per_block=tpb,
                  coarsen_factor=CoarsenFactor, thread_nz=max(1, int(ThreadNz) // G),
