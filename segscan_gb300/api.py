@@ -308,3 +308,47 @@ def segment_coo_sorted_sr(src, index, nnz, N, dst, *, CoarsenFactor, ThreadNz, D
     _ref_segment("sr", src, index, nnz, N, dst, group_factor=gf, thread_per_block=tpb,
                  coarsen_factor=CoarsenFactor, thread_nz=max(1, int(ThreadNz) // G),
                  block_numer=1, block_denom=1)
+
+
+# ---------------------------------------------------------------------------
+# Transpose, value gather, SDDMM (backward pass building blocks)
+# ---------------------------------------------------------------------------
+def transpose(A: CsrMatrix, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
+    """(A^T pattern with values gathered, perm): stable counting-sort transpose
+    on the device (dataloader.hpp:109-144); perm[q] = source nonzero of entry q."""
+    d = A.descr()
+    dev = A.indptr.device
+    n = ctypes.c_size_t()
+    _lib.call("ss_csr_transpose_workspace_size", ctypes.byref(d), ctypes.byref(n))
+    ws = _workspace(int(n.value), dev)
+    wp, wn = _aligned(ws)
+    t_indptr = torch.empty(A.ncol + 1, dtype=torch.int32, device=dev)
+    t_indices = torch.empty(A.nnz, dtype=torch.int32, device=dev)
+    perm = torch.empty(A.nnz, dtype=torch.int32, device=dev)
+    _lib.call("ss_csr_transpose", ctypes.byref(d), _ptr(t_indptr), _ptr(t_indices), _ptr(perm), wp, wn,
+              _stream(stream))
+    vals = None
+    if A.values is not None:
+        vals = gather_values(A.values, perm, stream)
+    return CsrMatrix(A.ncol, A.nrow, t_indptr, t_indices, vals), perm
+
+
+def gather_values(values: torch.Tensor, perm: torch.Tensor, stream=None) -> torch.Tensor:
+    _need_cuda("values", values)
+    _need_cuda("perm", perm, torch.int32)
+    out = torch.empty_like(values)
+    _lib.call("ss_gather_values", _ptr(values), int(dtype_code(values.dtype)), _ptr(perm), int(perm.numel()),
+              _ptr(out), _stream(stream))
+    return out
+
+
+def sddmm(A: CsrMatrix, dC: torch.Tensor, B: torch.Tensor, stream=None) -> torch.Tensor:
+    """dvals[p] = dot(dC[i, :], B[k, :]) at every stored nonzero p = (i, k); FP32."""
+    _need_cuda("dC", dC, torch.float32)
+    _need_cuda("B", B, A.dtype)
+    if dC.shape != (A.nrow, B.shape[1]) or B.shape[0] != A.ncol:
+        raise ValueError("dC must be [nrow, N] and B [ncol, N]")
+    out = torch.empty(A.nnz, dtype=torch.float32, device=dC.device)
+    d = A.descr()
+    _lib.call("ss_sddmm", ctypes.byref(d), int(B.shape[1]), _ptr(dC), _ptr(B), _ptr(out), _stream(stream))
+    return out

@@ -1,0 +1,71 @@
+"""Differentiable SpMM: a thin torch.autograd.Function over the C ABI.
+
+Forward: C = A @ B with one of the four strategies.  It saves only the
+sparse pattern, A's values and B; nothing is recomputed in backward.
+Backward:
+  dA.vals = SDDMM(dC, B)            (ss_sddmm: dot of dC row i with B row k)
+  dB      = A^T @ dC                (the forward kernels on A^T, whose
+                                     pattern is built on the device by the
+                                     stable counting-sort transpose once per
+                                     pattern and cached)
+Values stored in BF16/FP16 get FP32 gradients cast back to their dtype;
+dB is computed in FP32 (A^T values widened to FP32) and cast to B's dtype.
+This module is the training / test binding only; the library is the C ABI.
+"""
+from __future__ import annotations
+
+from typing import Optional
+
+import torch
+
+from . import api
+
+
+class _Pattern:
+    """A's pattern plus its lazily built transpose (cached across calls)."""
+
+    def __init__(self, A: api.CsrMatrix):
+        self.A = A.with_values(None)
+        self._t: Optional[tuple[api.CsrMatrix, torch.Tensor]] = None
+
+    def transposed(self) -> tuple[api.CsrMatrix, torch.Tensor]:
+        if self._t is None:
+            self._t = api.transpose(self.A)
+        return self._t
+
+
+class SpMMFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, values, B, pattern: _Pattern, strategy: str, knobs, bw_strategy: str):
+        A = pattern.A.with_values(values.contiguous())
+        C = api.spmm(A, B.contiguous(), strategy, knobs=knobs)
+        ctx.save_for_backward(values, B)
+        ctx.pattern = pattern
+        ctx.bw_strategy = bw_strategy
+        return C
+
+    @staticmethod
+    def backward(ctx, dC):
+        values, B = ctx.saved_tensors
+        pattern: _Pattern = ctx.pattern
+        dC = dC.contiguous().float()
+        d_values = d_B = None
+        if ctx.needs_input_grad[0]:
+            A = pattern.A.with_values(values)
+            d_values = api.sddmm(A, dC, B.contiguous()).to(values.dtype)
+        if ctx.needs_input_grad[1]:
+            AT, perm = pattern.transposed()
+            t_vals = api.gather_values(values.float().contiguous(), perm)
+            d_B = api.spmm(AT.with_values(t_vals), dC, ctx.bw_strategy).to(B.dtype)
+        return d_values, d_B, None, None, None, None
+
+
+def spmm(A: api.CsrMatrix, values: torch.Tensor, B: torch.Tensor, strategy: str = "ebsr", knobs=None,
+         bw_strategy: str = "ebsr", pattern: Optional[_Pattern] = None) -> torch.Tensor:
+    """C = A(values) @ B, differentiable in values and B."""
+    pattern = pattern or _Pattern(A)
+    return SpMMFunction.apply(values, B, pattern, strategy, knobs, bw_strategy)
+
+
+def pattern(A: api.CsrMatrix) -> _Pattern:
+    return _Pattern(A)

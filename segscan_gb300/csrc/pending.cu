@@ -2,9 +2,6 @@
 #include "internal.h"
 using namespace ss;
 extern "C" {
-ss_status ss_csr_transpose_workspace_size(const ss_csr *, size_t *) { return fail(SS_ERR_INVALID_ARG, "transpose not built"); }
-ss_status ss_csr_transpose(const ss_csr *, int32_t *, int32_t *, int32_t *, void *, size_t, void *) { return fail(SS_ERR_INVALID_ARG, "transpose not built"); }
-ss_status ss_sddmm(const ss_csr *, int, const float *, const void *, float *, void *) { return fail(SS_ERR_INVALID_ARG, "sddmm not built"); }
 ss_status ss_batch_plan_size(int, const ss_csr *, int, size_t *, size_t *) { return fail(SS_ERR_INVALID_ARG, "batched not built"); }
 ss_status ss_batch_plan(int, const ss_csr *, int, const void *const *, void *const *, int, const ss_knobs *, void *, size_t, void *, size_t, void *) { return fail(SS_ERR_INVALID_ARG, "batched not built"); }
 ss_status ss_spmm_batched(const void *, size_t, void *) { return fail(SS_ERR_INVALID_ARG, "batched not built"); }

@@ -1,0 +1,293 @@
+// Device CSR transpose (the backward pass's A^T) and value gather.
+//
+// Reference semantics: transpose + compressedRow
+// (test-cg/include/dataloader/dataloader.hpp:109-144), a stable counting
+// sort by column: entries of one column keep A's CSR order.  The device
+// version gives the same result bit for bit:
+//   1. column histogram (atomics)            -> counts
+//   2. exclusive scan of counts (3 kernels)  -> t_indptr
+//   3. scatter nonzero ids by column (atomic cursors; order inside a column
+//      is arbitrary here)                    -> perm
+//   4. sort each column's ids ascending      -> the stable order
+//      (thread insertion sort <= 32 entries, block bitonic sort in shared
+//      memory <= 16384, block bitonic sort in global memory beyond)
+//   5. t_indices[q] = row of perm[q]
+// Every step is deterministic given the input, so repeated calls agree.
+#include <algorithm>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace ss {
+
+constexpr int SCAN_TILE = 4096;  // elements per scan block (1024 threads x 4)
+constexpr int SMEM_SORT_MAX = 16384;
+
+struct TransposeWs {
+  int32_t *counts;    // [K + 1]
+  int32_t *cursor;    // [K]
+  int32_t *bsum;      // [SCAN_TILE]
+  int32_t *rowid;     // [nnz]
+  int32_t *work;      // [1 + K]: count, then column ids with > 32 entries
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static size_t transpose_ws_bytes(int K, int nnz, TransposeWs *w, void *base) {
+  size_t o = 0;
+  const size_t counts = o; o += align256((size_t)(K + 1) * 4);
+  const size_t cursor = o; o += align256((size_t)K * 4);
+  const size_t bsum = o; o += align256((size_t)SCAN_TILE * 4);
+  const size_t rowid = o; o += align256((size_t)nnz * 4);
+  const size_t work = o; o += align256((size_t)(K + 1) * 4);
+  if (w) {
+    char *b = (char *)base;
+    w->counts = (int32_t *)(b + counts);
+    w->cursor = (int32_t *)(b + cursor);
+    w->bsum = (int32_t *)(b + bsum);
+    w->rowid = (int32_t *)(b + rowid);
+    w->work = (int32_t *)(b + work);
+  }
+  return o;
+}
+
+static int grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b > 152 * 32) b = 152 * 32;
+  return b < 1 ? 1 : (int)b;
+}
+
+__global__ void hist_kernel(const int32_t *__restrict__ cols, int nnz, int K, int32_t *counts) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nnz; p += (long long)gridDim.x * blockDim.x) {
+    const int c = cols[p];
+    if ((unsigned)c < (unsigned)K) atomicAdd(counts + c, 1);
+  }
+}
+
+// Block-wide exclusive scan of SCAN_TILE ints: out = exclusive prefix, and
+// the tile total to bsum[blockIdx.x].
+__global__ void __launch_bounds__(1024) scan_tile_kernel(const int32_t *__restrict__ in, int n, int32_t *out,
+                                                         int32_t *bsum) {
+  __shared__ int32_t warp_tot[32];
+  const int base = blockIdx.x * SCAN_TILE + threadIdx.x * 4;
+  int v[4];
+  #pragma unroll
+  for (int i = 0; i < 4; i++) v[i] = base + i < n ? in[base + i] : 0;
+  int t = v[0] + v[1] + v[2] + v[3];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = t;
+  #pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+    int wi = w;
+    #pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, wi, off);
+      if (lane >= off) wi += y;
+    }
+    warp_tot[lane] = wi - w;  // exclusive prefix of warp totals
+    if (lane == 31) bsum[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  int run = warp_tot[wid] + incl - t;
+  #pragma unroll
+  for (int i = 0; i < 4; i++) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+}
+
+// out[i] += prefix of bsum before i's tile; bsum is scanned in place by
+// block 0 first (at most SCAN_TILE tiles).
+__global__ void __launch_bounds__(1024) scan_bsum_kernel(int32_t *bsum, int nb, int32_t *total) {
+  __shared__ int32_t warp_tot[32];
+  const int base = threadIdx.x * 4;
+  int v[4];
+  #pragma unroll
+  for (int i = 0; i < 4; i++) v[i] = base + i < nb ? bsum[base + i] : 0;
+  const int t = v[0] + v[1] + v[2] + v[3];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = t;
+  #pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int w = warp_tot[lane];
+    int wi = w;
+    #pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, wi, off);
+      if (lane >= off) wi += y;
+    }
+    warp_tot[lane] = wi - w;
+    if (lane == 31) *total = wi;
+  }
+  __syncthreads();
+  int run = warp_tot[wid] + incl - t;
+  #pragma unroll
+  for (int i = 0; i < 4; i++) {
+    if (base + i < nb) bsum[base + i] = run;
+    run += v[i];
+  }
+}
+
+__global__ void scan_add_kernel(int32_t *out, int n, const int32_t *__restrict__ bsum) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] += bsum[i / SCAN_TILE];
+}
+
+__global__ void scatter_kernel(const int32_t *__restrict__ cols, int nnz, int K, int32_t *cursor, int32_t *perm) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nnz; p += (long long)gridDim.x * blockDim.x) {
+    const int c = cols[p];
+    if ((unsigned)c < (unsigned)K) {
+      const int q = atomicAdd(cursor + c, 1);
+      perm[q] = (int32_t)p;
+    }
+  }
+}
+
+// Thread per column: insertion sort of short columns, queue the rest.
+__global__ void sort_small_kernel(const int32_t *__restrict__ t_indptr, int K, int32_t *perm, int32_t *work) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < K; c += (long long)gridDim.x * blockDim.x) {
+    const int s = t_indptr[c], e = t_indptr[c + 1];
+    const int n = e - s;
+    if (n <= 1) continue;
+    if (n > 32) {
+      const int slot = atomicAdd(work, 1);
+      work[1 + slot] = (int32_t)c;
+      continue;
+    }
+    int32_t *a = perm + s;
+    for (int i = 1; i < n; i++) {
+      const int32_t x = a[i];
+      int j = i - 1;
+      while (j >= 0 && a[j] > x) {
+        a[j + 1] = a[j];
+        j--;
+      }
+      a[j + 1] = x;
+    }
+  }
+}
+
+// Ascending bitonic sort of n keys at `a` (shared or global), padded to
+// the next power of two with virtual +inf keys.  The first step of every
+// merge stage compares mirrored positions, so all comparisons put the
+// smaller key at the lower index and a padded (+inf) partner never moves.
+__device__ __forceinline__ void bitonic_block(int32_t *a, int n) {
+  int P = 1;
+  while (P < n) P <<= 1;
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
+        if (partner > i && partner < n) {
+          const int32_t x = a[i], y = a[partner];
+          if (x > y) {
+            a[i] = y;
+            a[partner] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(1024) sort_large_kernel(const int32_t *__restrict__ t_indptr, int32_t *perm,
+                                                          const int32_t *__restrict__ work) {
+  extern __shared__ int32_t keys[];
+  const int count = work[0];
+  for (int w = blockIdx.x; w < count; w += gridDim.x) {
+    const int c = work[1 + w];
+    const int s = t_indptr[c], n = t_indptr[c + 1] - s;
+    if (n <= SMEM_SORT_MAX) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = perm[s + i];
+      __syncthreads();
+      bitonic_block(keys, n);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) perm[s + i] = keys[i];
+      __syncthreads();
+    } else {
+      bitonic_block(perm + s, n);  // in global memory; rare
+      __syncthreads();
+    }
+  }
+}
+
+// rowid[p] = row of nonzero p (binary_search_segment_number semantics)
+__global__ void rowid_kernel(const int32_t *__restrict__ indptr, int M, int nnz, int32_t *rowid) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nnz; p += (long long)gridDim.x * blockDim.x)
+    rowid[p] = row_search(indptr, 1, M, (int)p);
+}
+
+__global__ void gather_rows_kernel(const int32_t *__restrict__ perm, const int32_t *__restrict__ rowid, int nnz,
+                                   int32_t *t_indices) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x)
+    t_indices[q] = rowid[perm[q]];
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" {
+
+ss_status ss_csr_transpose_workspace_size(const ss_csr *A, size_t *bytes) {
+  if (!A || !bytes || A->nrow < 0 || A->ncol < 0 || A->nnz < 0) return fail(SS_ERR_INVALID_ARG, "bad arguments");
+  *bytes = transpose_ws_bytes(A->ncol, A->nnz, nullptr, nullptr);
+  return SS_OK;
+}
+
+ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indices, int32_t *perm, void *ws,
+                           size_t ws_bytes, void *stream) {
+  if (!A || A->nrow < 0 || A->ncol < 0 || A->nnz < 0) return fail(SS_ERR_INVALID_ARG, "bad CSR descriptor");
+  const int M = A->nrow, K = A->ncol, nnz = A->nnz;
+  if (!t_indptr || (nnz > 0 && (!t_indices || !perm || !A->indices || !A->indptr)))
+    return fail(SS_ERR_INVALID_ARG, "null pointer");
+  const long long tiles = ((long long)K + SCAN_TILE - 1) / SCAN_TILE;
+  if (tiles > SCAN_TILE) return fail(SS_ERR_CAPACITY, "ncol %d above the scan capacity %d", K, SCAN_TILE * SCAN_TILE);
+  const size_t need = transpose_ws_bytes(K, nnz, nullptr, nullptr);
+  if (ws_bytes < need || !ws || ((uintptr_t)ws % 256))
+    return fail(SS_ERR_WORKSPACE, "workspace needs %zu bytes (256-byte aligned), got %zu", need, ws_bytes);
+  TransposeWs w;
+  transpose_ws_bytes(K, nnz, &w, ws);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(w.counts, 0, (size_t)(K + 1) * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.work, 0, 4, s);
+  if (e != cudaSuccess) return cuda_fail(e, "transpose clear");
+  if (K == 0) return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose");
+  if (nnz > 0) hist_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indices, nnz, K, w.counts);
+  scan_tile_kernel<<<(int)tiles, 1024, 0, s>>>(w.counts, K, t_indptr, w.bsum);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, (int)tiles, t_indptr + K);
+  scan_add_kernel<<<grid_for(K, 256), 256, 0, s>>>(t_indptr, K, w.bsum);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "transpose scan");
+  if (nnz == 0) return SS_OK;
+  e = cudaMemcpyAsync(w.cursor, t_indptr, (size_t)K * 4, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "transpose cursor");
+  scatter_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indices, nnz, K, w.cursor, perm);
+  sort_small_kernel<<<grid_for(K, 256), 256, 0, s>>>(t_indptr, K, perm, w.work);
+  static bool attr_set = false;
+  if (!attr_set) {
+    e = cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_SORT_MAX * 4);
+    if (e != cudaSuccess) return cuda_fail(e, "transpose sort attribute");
+    attr_set = true;
+  }
+  sort_large_kernel<<<2 * 152, 1024, SMEM_SORT_MAX * 4, s>>>(t_indptr, perm, w.work);
+  rowid_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indptr, M, nnz, w.rowid);
+  gather_rows_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(perm, w.rowid, nnz, t_indices);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
+}
+
+}  // extern "C"
