@@ -232,8 +232,11 @@ __global__ void rowid_kernel(const int32_t *__restrict__ indptr, int M, int nnz,
 
 __global__ void gather_rows_kernel(const int32_t *__restrict__ perm, const int32_t *__restrict__ rowid, int nnz,
                                    int32_t *t_indices) {
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x)
-    t_indices[q] = rowid[perm[q]];
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x) {
+    // entries past t_indptr[K] exist only when A has out-of-range columns
+    const int p = perm[q];
+    t_indices[q] = (unsigned)p < (unsigned)nnz ? rowid[p] : -1;
+  }
 }
 
 }  // namespace ss
@@ -277,12 +280,8 @@ ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indice
   if (e != cudaSuccess) return cuda_fail(e, "transpose cursor");
   scatter_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indices, nnz, K, w.cursor, perm);
   sort_small_kernel<<<grid_for(K, 256), 256, 0, s>>>(t_indptr, K, perm, w.work);
-  static bool attr_set = false;
-  if (!attr_set) {
-    e = cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_SORT_MAX * 4);
-    if (e != cudaSuccess) return cuda_fail(e, "transpose sort attribute");
-    attr_set = true;
-  }
+  e = cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_SORT_MAX * 4);
+  if (e != cudaSuccess) return cuda_fail(e, "transpose sort attribute");
   sort_large_kernel<<<2 * 152, 1024, SMEM_SORT_MAX * 4, s>>>(t_indptr, perm, w.work);
   rowid_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indptr, M, nnz, w.rowid);
   gather_rows_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(perm, w.rowid, nnz, t_indices);

@@ -47,7 +47,7 @@ __global__ void index_validate_kernel(const int32_t *__restrict__ index, int nnz
 template <typename T>
 __global__ void gather_kernel(const T *__restrict__ in, const int32_t *__restrict__ perm, int n, T *__restrict__ out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = in[perm[i]];
+    out[i] = (unsigned)perm[i] < (unsigned)n ? in[perm[i]] : T(0);
 }
 
 static int grid_for(int64_t n, int threads) {
