@@ -153,14 +153,17 @@ def dist_setup(args):
 
 
 def cpu_spmm_time(A, B, threads: int, budget_s: float, min_iters: int = 2, max_iters: int = 50):
-    """Times the reference's CPU SpMM (oracle port) on A, B: seconds per pass."""
+    """Times the reference's CPU SpMM (oracle port: zero C, then the check-path
+    loop, a row block per thread) on A, B: seconds per pass."""
     sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
     import oracle_lib
+    out = np.empty((A.nrow, B.shape[1]), dtype=np.float32)
     times = []
     start = time.perf_counter()
     while len(times) < max_iters:
         t0 = time.perf_counter()
-        oracle_lib.spmm_check_f32(A.indptr, A.indices, A.values, B, threads=threads)
+        oracle_lib.spmm_check_f32(A.indptr, A.indices, A.values, B, threads=threads, out=out)
         times.append(time.perf_counter() - t0)
         if len(times) >= min_iters and time.perf_counter() - start > budget_s:
             break
@@ -189,13 +192,15 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     sample, desc, _ = cpu_sample(A, B, 2.0, threads)
     nbytes = synth.spmm_bytes(sample, args.N)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+    import oracle_lib
+    out = np.empty((sample.nrow, args.N), dtype=np.float32)
     for _ in range(max(0, args.warmup)):
-        cpu_spmm_time(sample, B, threads, 0.0, 1, 1)
+        oracle_lib.spmm_check_f32(sample.indptr, sample.indices, sample.values, B, threads=threads, out=out)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import oracle_lib
-        oracle_lib.spmm_check_f32(sample.indptr, sample.indices, sample.values, B, threads=threads)
+        oracle_lib.spmm_check_f32(sample.indptr, sample.indices, sample.values, B, threads=threads, out=out)
     dt = (time.perf_counter() - t0) / args.steps
     gbs = nbytes / dt / 1e9
     line = {"metric": METRIC, "value": gbs, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,

@@ -63,6 +63,7 @@ EXPORT void oracle_spmm_check_f32(int M, int N, const int32_t *indptr,
 typedef struct {
   int64_t r0, r1;
   int N;
+  int zero;
   const int32_t *indptr, *indices;
   const float *vals, *B;
   float *C;
@@ -70,14 +71,34 @@ typedef struct {
 
 static void *spmm_job_run(void *arg) {
   spmm_job *j = (spmm_job *)arg;
+  if (j->zero)  /* out_ref.fill_zero_h() for this thread's rows */
+    memset(j->C + j->r0 * (int64_t)j->N, 0, (size_t)(j->r1 - j->r0) * (size_t)j->N * sizeof(float));
   spmm_check_rows(j->r0, j->r1, j->N, j->indptr, j->indices, j->vals, j->B, j->C);
   return NULL;
 }
 
+static void spmm_check_mt(int M, int N, const int32_t *indptr, const int32_t *indices, const float *vals,
+                          const float *B, float *C, int nthreads, int zero);
+
 EXPORT void oracle_spmm_check_f32_mt(int M, int N, const int32_t *indptr,
                                      const int32_t *indices, const float *vals,
                                      const float *B, float *C, int nthreads) {
+  spmm_check_mt(M, N, indptr, indices, vals, B, C, nthreads, 0);
+}
+
+/* C = 0; C += A*B with every thread zeroing and then filling its own row
+ * block (the timed CPU baseline: zero fill and loop, as the reference's
+ * check mode does them). */
+EXPORT void oracle_spmm_f32_zero_mt(int M, int N, const int32_t *indptr,
+                                    const int32_t *indices, const float *vals,
+                                    const float *B, float *C, int nthreads) {
+  spmm_check_mt(M, N, indptr, indices, vals, B, C, nthreads, 1);
+}
+
+static void spmm_check_mt(int M, int N, const int32_t *indptr, const int32_t *indices, const float *vals,
+                          const float *B, float *C, int nthreads, int zero) {
   if (nthreads <= 1 || M < 2 * nthreads) {
+    if (zero) memset(C, 0, (size_t)M * (size_t)N * sizeof(float));
     oracle_spmm_check_f32(M, N, indptr, indices, vals, B, C);
     return;
   }
@@ -102,7 +123,7 @@ EXPORT void oracle_spmm_check_f32_mt(int M, int N, const int32_t *indptr,
       r1 = lo + 1 > M ? M : lo + 1;
       if (r1 < r) r1 = r;
     }
-    jobs[t].r0 = r; jobs[t].r1 = r1; jobs[t].N = N;
+    jobs[t].r0 = r; jobs[t].r1 = r1; jobs[t].N = N; jobs[t].zero = zero;
     jobs[t].indptr = indptr; jobs[t].indices = indices; jobs[t].vals = vals;
     jobs[t].B = B; jobs[t].C = C;
     r = r1;

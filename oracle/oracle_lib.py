@@ -38,20 +38,28 @@ def _p(a):
     return None if a is None else a.ctypes.data_as(c_void_p)
 
 
-def spmm_check_f32(indptr, indices, vals, B, threads: int = 1):
-    """The reference's CPU check path (check.cuh:139-158): C = 0; C += A*B in FP32."""
+def spmm_check_f32(indptr, indices, vals, B, threads: int = 1, out=None):
+    """The reference's CPU check path (check.cuh:139-158): C = 0; C += A*B in FP32.
+    With `out` the result goes there (zeroed inside, row block per thread)."""
     M = indptr.size - 1
     N = B.shape[1]
-    C = np.zeros((M, N), dtype=np.float32)
     lib = load()
-    args = (c_int(M), c_int(N), _p(np.ascontiguousarray(indptr, np.int32)),
-            _p(np.ascontiguousarray(indices, np.int32)), _p(np.ascontiguousarray(vals, np.float32)),
-            _p(np.ascontiguousarray(B, np.float32)), _p(C))
-    if threads > 1:
-        lib.oracle_spmm_check_f32_mt(*args, c_int(threads))
-    else:
-        lib.oracle_spmm_check_f32(*args)
-    return C
+    if out is None:
+        C = np.zeros((M, N), dtype=np.float32)
+        args = (c_int(M), c_int(N), _p(np.ascontiguousarray(indptr, np.int32)),
+                _p(np.ascontiguousarray(indices, np.int32)), _p(np.ascontiguousarray(vals, np.float32)),
+                _p(np.ascontiguousarray(B, np.float32)), _p(C))
+        if threads > 1:
+            lib.oracle_spmm_check_f32_mt(*args, c_int(threads))
+        else:
+            lib.oracle_spmm_check_f32(*args)
+        return C
+    assert out.dtype == np.float32 and out.shape == (M, N) and out.flags.c_contiguous
+    lib.oracle_spmm_f32_zero_mt(c_int(M), c_int(N), _p(np.ascontiguousarray(indptr, np.int32)),
+                                _p(np.ascontiguousarray(indices, np.int32)),
+                                _p(np.ascontiguousarray(vals, np.float32)), _p(np.ascontiguousarray(B, np.float32)),
+                                _p(out), c_int(threads))
+    return out
 
 
 def spmm_f64(indptr, indices, vals, B):
