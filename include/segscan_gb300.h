@@ -157,6 +157,19 @@ ss_status ss_spmm_ebsr(const ss_csr *A, int N, const void *B, void *C,
                        int c_dtype, int accumulate, const ss_knobs *knobs,
                        void *ws, size_t ws_bytes, void *stream);
 
+/* The ebsr SpMM without a workspace argument, for callers that cannot
+ * allocate device memory: a host that only holds buffers handed to it by
+ * another allocator, or a loop where cudaMalloc's blocking, device
+ * synchronisation or failure is not acceptable.  Its scratch is a fixed
+ * 16 MiB array inside the library (held on every GPU that loads it); calls
+ * needing more get SS_ERR_CAPACITY.  All calls on a device share that array,
+ * so calls that overlap on the GPU race.  The first call on a device looks
+ * up the array's address; make it before any stream capture.  No
+ * counterpart in the reference. */
+ss_status ss_spmm_ebsr_noalloc(const ss_csr *A, int N, const void *B, void *C,
+                               int c_dtype, int accumulate,
+                               const ss_knobs *knobs, void *stream);
+
 /* Replaces csrspmm_seqreduce_rowbalance_cg<Index, DType, coarsen_factor,
  * thread_per_block, tile_factor, block_numer, block_denom>
  * (spmm_cg.cuh:664-666). */

@@ -91,6 +91,8 @@ _SIGNATURES = {
                              c_void_p, c_size_t, c_void_p]),
     "ss_spmm": (c_int, [c_int, POINTER(SsCsr), c_int, c_void_p, c_void_p, c_int, c_int, POINTER(SsKnobs),
                         c_void_p, c_size_t, c_void_p]),
+    "ss_spmm_ebsr_noalloc": (c_int, [POINTER(SsCsr), c_int, c_void_p, c_void_p, c_int, c_int,
+                                     POINTER(SsKnobs), c_void_p]),
     "ss_segment_coo_workspace_size": (c_int, [c_int, c_int, c_int, POINTER(SsKnobs), POINTER(c_size_t)]),
     "ss_segment_coo": (c_int, [c_int, c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_int,
                                c_int, POINTER(SsKnobs), c_void_p, c_size_t, c_void_p]),

@@ -1,0 +1,53 @@
+"""ss_spmm_ebsr_noalloc: the ebsr SpMM for callers that cannot allocate device
+memory (a host that only holds buffers handed to it by another allocator, or
+a loop where cudaMalloc cannot be called), whose scratch is a fixed array
+inside the library.  This file is collected last on purpose."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import check_close, dev_csr, oracle64
+from segscan_gb300 import synth
+from segscan_gb300._lib import SsCsr, SsKnobs, Status
+
+
+def call_noalloc(lib, A, N, B, C, knobs):
+    d = A.descr()
+    return lib.ss_spmm_ebsr_noalloc(ctypes.byref(d), N, B.data_ptr(), C.data_ptr(), 0, 0, ctypes.byref(knobs),
+                                    torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.mark.gpu
+def test_noalloc_matches_workspace_entry_point(cuda, lib):
+    """Two calls in a row on different matrices (the second sees the first's
+    leftovers in the shared array); each must agree with ss_spmm_ebsr run
+    with a caller workspace, at the SpMM tolerance (1e-5 of sum|a*b|)."""
+    from segscan_gb300 import api
+    N = 64
+    for seed in (21, 22):
+        csr = synth.powerlaw(30000, 30000, 2.1, 1, 3000, seed=seed)
+        B = synth.dense(csr.ncol, N, seed=seed + 100)
+        A = dev_csr(csr)
+        Bd = torch.from_numpy(B).cuda()
+        knobs = api.make_knobs("ebsr", N, group_factor=4, thread_nz=8, block_denom=1)
+        ref = api.spmm(A, Bd, "ebsr", knobs=knobs)
+        out = torch.full_like(ref, float("nan"))
+        st = call_noalloc(lib, A, N, Bd, out, knobs)
+        assert st == Status.OK, lib.ss_last_error()
+        torch.cuda.synchronize()
+        C64, absC = oracle64(csr, B)
+        got, want = out.cpu().numpy(), ref.cpu().numpy()
+        check_close(got, want.astype(np.float64), absC, 1e-5, None, f"noalloc vs workspace entry, seed {seed}")
+        check_close(got, C64, absC, 1e-5, 1e-5, f"noalloc vs FP64, seed {seed}")
+
+
+def test_noalloc_rejects_oversize_scratch(lib):
+    """A call whose scratch would exceed the fixed array is refused before any
+    device work (the pointers here are never dereferenced)."""
+    big = SsCsr(4_000_000, 4_000_000, 400_000_000, 256, 512, 1024, 0)
+    knobs = SsKnobs(4, 0, 256, 1, 1, 4, 1, 0)  # 16-nonzero chunks: 25 M chunks of carries
+    st = lib.ss_spmm_ebsr_noalloc(ctypes.byref(big), 64, 4096, 8192, 0, 0, ctypes.byref(knobs), None)
+    assert st == Status.CAPACITY
+    assert b"fixed" in lib.ss_last_error()
