@@ -178,15 +178,13 @@ static ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int 
   g.block = k.thread_per_block;
   g.chunk = k.thread_nz * G;
   g.num_chunks = nnz > 0 ? ceil_div(nnz, g.chunk) : 0;
-  // staged tile: 64 nonzeros, halved while the block's groups would need
-  // more than 96 KB of shared memory, but never below the 16 nonzeros the
-  // SpMM gather ring runs ahead (a multiple of 8 also keeps bulk copies
+  // staged tile: 64 nonzeros, smaller when the block's groups would need
+  // more than 48 KB of shared memory (a multiple of 8 keeps bulk copies
   // 16-byte aligned)
-  const int ring = val_bytes > 0 ? sr_ring_bytes(G, g.cs.V, g.cs.NV, val_bytes) : 0;
   int stage = 64;
-  while (stage > 16 && sr_smem_bytes(stage, g.workers_per_block, val_bytes, ring) > 96 * 1024) stage >>= 1;
+  while (stage > 8 && sr_smem_bytes(stage, g.workers_per_block, val_bytes) > 48 * 1024) stage >>= 1;
   g.stage = stage;
-  g.smem = sr_smem_bytes(stage, g.workers_per_block, val_bytes, ring);
+  g.smem = sr_smem_bytes(stage, g.workers_per_block, val_bytes);
   if (g.smem > 200 * 1024)
     return fail(SS_ERR_UNSUPPORTED_KNOBS, "%d groups per block need %zu B of shared memory",
                 g.workers_per_block, g.smem);

@@ -19,12 +19,9 @@ static int *walk_error_ptr() {
 // ---------------------------------------------------------------------
 EbArgs eb_base_args(const EbGeom &g, void *ws, int N);
 
-size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes, int ring_bytes) {
-  return (size_t)workers_per_block * (size_t)sr_layout(stage, val_bytes, ring_bytes).bytes;
+size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes) {
+  return (size_t)workers_per_block * (size_t)sr_layout(stage, val_bytes).bytes;
 }
-
-// bytes of one group's gather ring (SpMM walk)
-int sr_ring_bytes(int G, int V, int NV, int val_bytes) { return SR_R * G * V * NV * val_bytes; }
 
 static int sm_count() {
   static int n = 0;
@@ -73,10 +70,8 @@ ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
   if (c.val_dtype == SS_F32) fn = sr_kernel_f32(g.cs.V, g.cs.NV, false);
   else if (c.val_dtype == SS_BF16) fn = sr_kernel_bf16(g.cs.V, g.cs.NV, false, c.c_dtype == SS_F32);
   else fn = sr_kernel_f16(g.cs.V, g.cs.NV, false, c.c_dtype == SS_F32);
-  const int vb = dtype_size(c.val_dtype);
-  ss_status st = run_sr(fn, a, g,
-                        sr_smem_bytes(g.stage, g.workers_per_block, vb, sr_ring_bytes(g.team_lanes, g.cs.V, g.cs.NV, vb)),
-                        s, "ebsr launch");
+  ss_status st = run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, dtype_size(c.val_dtype)), s,
+                        "ebsr launch");
   if (st != SS_OK) return st;
   return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.M, c.C, c.c_dtype, SS_SUM,
                       c.accumulate, nullptr, c.nnz, s);
@@ -93,7 +88,7 @@ ss_status launch_seg_sr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_
   if (c.src_dtype == SS_F32) fn = sr_kernel_f32(g.cs.V, g.cs.NV, true);
   else if (c.src_dtype == SS_BF16) fn = sr_kernel_bf16(g.cs.V, g.cs.NV, true, true);
   else fn = sr_kernel_f16(g.cs.V, g.cs.NV, true, true);
-  ss_status st = run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, 0, 0), s, "segment_coo sr launch");
+  ss_status st = run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, 0), s, "segment_coo sr launch");
   if (st != SS_OK) return st;
   return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce,
                       c.accumulate, c.index, c.nnz, s);

@@ -31,20 +31,18 @@
 
 namespace ss {
 
-constexpr int SR_U = 4;                       // B rows gathered ahead (segment walk)
-constexpr int SR_R = 16;                      // B rows in flight per group (SpMM ring)
+constexpr int SR_U = 4;                       // B rows gathered ahead
 constexpr uint32_t SR_SPIN_LIMIT = 1u << 22;  // try_wait polls before giving up
 
 // Per-group shared memory: [bar0 bar1 | col[2][S] | val[2][S] | win[W]]
 struct SrLayout {
   int S, W, vs;
-  int col_off, val_off, info_off, win_off, ring_off, bytes;
+  int col_off, val_off, info_off, win_off, bytes;
 };
 
 // Per-group shared memory: [bar0 bar1 | col[2][S] | val[2][S] | info[2][S] |
-// win[W] | ring].  info holds, per staged nonzero, its row and an
-// end-of-row bit; ring holds the gathered B slices in flight (SpMM).
-__host__ __device__ inline SrLayout sr_layout(int S, int vs, int ring_bytes = 0) {
+// win[W]].  info holds, per staged nonzero, its row and an end-of-row bit.
+__host__ __device__ inline SrLayout sr_layout(int S, int vs) {
   SrLayout L;
   L.S = S;
   L.W = 2 * S + 8;
@@ -58,9 +56,6 @@ __host__ __device__ inline SrLayout sr_layout(int S, int vs, int ring_bytes = 0)
   o += 2 * S * 4;
   L.win_off = o;
   o += L.W * 4;
-  o = (o + 15) & ~15;
-  L.ring_off = o;
-  o += ring_bytes;
   L.bytes = (o + 15) & ~15;
   return L;
 }
@@ -141,64 +136,6 @@ __device__ __forceinline__ int group_lower_bound(const int32_t *indptr, int M, i
   return lo;
 }
 
-// Asynchronous global -> shared copy of BYTES (4, 8 or 16) by this lane;
-// completion is tracked per thread with commit / wait groups.
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void *dst, const void *src, uint64_t pol) {
-  if constexpr (BYTES == 16) {
-    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
-                 "l"(pol) : "memory");
-  } else {
-    static_assert(BYTES == 8 || BYTES == 4, "cp.async moves 4, 8 or 16 bytes");
-    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], %2, %3;" ::"r"(smem_u32(dst)), "l"(src),
-                 "n"(BYTES), "l"(pol) : "memory");
-  }
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
-// Starts the copy of this lane's E = V*NV elements of B row c into ring
-// slot dst (zeros when c is out of range or the lane has no columns).
-template <typename T, int V, int NV>
-__device__ __forceinline__ void ring_issue(T *dst, const T *__restrict__ B, int c, int K, int N, int col0,
-                                           const bool (&act)[NV], uint64_t pol) {
-  constexpr int BYTES = V * (int)sizeof(T);
-  const bool live = (unsigned)c < (unsigned)K;
-  #pragma unroll
-  for (int j = 0; j < NV; j++) {
-    if (!act[j]) continue;
-    T *d = dst + j * V;
-    if (live) {
-      const T *src = B + (int64_t)c * N + col0 + j * V;
-      if constexpr (BYTES >= 4) {
-        cp_async<BYTES>(d, src, pol);
-      } else {
-        *d = *src;  // 2-byte slice: synchronous
-      }
-    } else {
-      #pragma unroll
-      for (int i = 0; i < V; i++) d[i] = T(0.f);
-    }
-  }
-}
-
-template <typename T, int V, int NV>
-__device__ __forceinline__ void ring_read(const T *src, float (&b)[NV][V]) {
-  #pragma unroll
-  for (int j = 0; j < NV; j++) {
-    if constexpr (sizeof(T) == 4 && V == 4) {
-      const float4 x = *reinterpret_cast<const float4 *>(src + j * V);
-      b[j][0] = x.x; b[j][1] = x.y; b[j][2] = x.z; b[j][3] = x.w;
-    } else {
-      #pragma unroll
-      for (int i = 0; i < V; i++) b[j][i] = Elem<T>::to_f(src[j * V + i]);
-    }
-  }
-}
-
 template <int V, int NV, bool KAHAN>
 __device__ __forceinline__ void add_row(float (&acc)[NV][V], float (&comp)[NV][V], float v,
                                         const float (&b)[NV][V]) {
@@ -242,23 +179,19 @@ __device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)
   }
 }
 
-// Returns false when a bounded wait expired (the kernel then stops).
 template <typename T, typename TC, int V, int NV, bool KAHAN>
-__device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
-                                              const SrLayout &L, T *ring, int col0, const bool (&act)[NV],
-                                              uint64_t keep, uint64_t strm) {
+__device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
+                                              const SrLayout &L, int col0, const bool (&act)[NV], uint64_t keep,
+                                              uint64_t strm) {
   const T *__restrict__ B = (const T *)a.B;
   const int G = a.team_lanes;
-  constexpr int E = V * NV;
   const bool ones = a.vals == nullptr;
   ChunkInfo ci;
   ci.cs = chunk * a.chunk;
   ci.ce = min(ci.cs + a.chunk, a.nnz);
-  const int nel = ci.ce - ci.cs;
-  const int S = L.S;
-  const int nst = (nel + S - 1) / S;
-  stage_issue<T, false>(a, st, L, 0, ci.cs, min(S, nel), lane, G, mask, strm);
-  if (nst > 1) stage_issue<T, false>(a, st, L, 1, ci.cs + S, min(S, nel - S), lane, G, mask, strm);
+  const int nst = (ci.ce - ci.cs + L.S - 1) / L.S;
+  stage_issue<T, false>(a, st, L, 0, ci.cs, min(L.S, ci.ce - ci.cs), lane, G, mask, strm);
+  if (nst > 1) stage_issue<T, false>(a, st, L, 1, ci.cs + L.S, min(L.S, ci.ce - ci.cs - L.S), lane, G, mask, strm);
 
   // first row: lb = first row starting at or after cs
   const int lb = group_lower_bound(a.indptr, a.M, ci.cs, lane, G, mask);
@@ -314,138 +247,138 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
       for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
   };
 
-  // B slices are gathered into this lane's ring SR_R nonzeros ahead
-  T *my_ring = ring + (size_t)lane * E;
-  const int ring_stride = G * E;  // elements between consecutive slots
-  int waited = 0;                 // tiles whose bulk copy has been waited for
-  bool ok = true;
-  auto issue = [&](int e) {
-    if (e >= nel) return;
-    const int t = e / S;
-    if (t >= waited) {  // first use of tile t: its columns must have landed
-      if (!stage_wait(st, t & 1, mask, a.err)) ok = false;
-      waited = t + 1;
-    }
-    const int c = st.col[(t & 1) * S + (e - t * S)];
-    ring_issue<T, V, NV>(my_ring + (size_t)(e % SR_R) * ring_stride, B, c, a.K, a.N, col0, act, keep);
-  };
-  #pragma unroll 1
-  for (int e = 0; e < SR_R - 1; e++) {
-    issue(e);
-    cp_async_commit();
-  }
+  for (int s = 0; s < nst; s++) {
+    const int b = s & 1;
+    const int sb = ci.cs + s * L.S;
+    const int n = min(L.S, ci.ce - sb);
+    const int last = sb + n - 1;
+    if (!stage_wait(st, b, mask, a.err)) return;
+    const int32_t *scol = st.col + b * L.S;
+    const T *sval = reinterpret_cast<const T *>(st.val + b * L.S * L.vs);
+    int32_t *sinfo = st.info + b * L.S;
 
-  bool fast = true;
-  int next_start = 0;
-  int tile_last = -1;  // global index of the current tile's last nonzero
-  for (int e = 0; e < nel && ok; e++) {
-    issue(e + SR_R - 1);
-    cp_async_commit();
-    const int t = e / S;
-    const int q = e - t * S;
-    const int b = t & 1;
-    const int sb = ci.cs + t * S;
-    if (q == 0) {
-      // ---- a new tile: decide how its rows are tracked
-      const int n = min(S, nel - t * S);
-      const int last = sb + n - 1;
-      tile_last = last;
-      if (cur < win_base || st.win[L.W - 1] <= last) win_fill(cur);
-      fast = st.win[L.W - 1] > last || win_base + L.W - 1 >= a.M;
-      if (fast) {
-        // label the tile's nonzeros with row | end-of-row bit; empty rows
-        // starting where a row's first nonzero sits are zeroed by the whole
-        // group (each lane owns one column slice)
-        int32_t *sinfo = st.info + b * S;
-        const int c0 = cur - win_base;
-        const int rounds = (n + G - 1) / G;
-        for (int k = 0; k < rounds; k++) {
-          const int el = lane + k * G;
-          int zlo = 0, zhi = -1;
-          if (el < n) {
-            const int p = sb + el;
-            int lo = c0 + 1, hi = L.W - 1;
-            while (lo < hi) {
-              const int mid = (lo + hi) >> 1;
-              if (st.win[mid] <= p) lo = mid + 1; else hi = mid;
-            }
-            const int rr = lo - 1;
-            const bool end = st.win[rr + 1] == p + 1;
-            sinfo[el] = (win_base + rr) | (end ? (int)0x80000000 : 0);
-            if (st.win[rr] == p && p != ci.cs) {
-              int qq = rr - 1;
-              while (qq > c0 && st.win[qq] == p) qq--;
-              zlo = win_base + qq + 1;
-              zhi = win_base + rr - 1;
-            }
+    // the window must hold the starts of every row this tile touches and of
+    // the row after the last one
+    if (cur < win_base || st.win[L.W - 1] <= last) win_fill(cur);
+    const bool fast = st.win[L.W - 1] > last || win_base + L.W - 1 >= a.M;
+
+    if (fast) {
+      // ---- label the tile's nonzeros with row | end-of-row bit; empty rows
+      // starting where a row's first nonzero sits are zeroed by the whole
+      // group (each lane owns one column slice)
+      const int c0 = cur - win_base;
+      const int rounds = (n + G - 1) / G;
+      for (int k = 0; k < rounds; k++) {
+        const int e = lane + k * G;
+        int zlo = 0, zhi = -1;
+        if (e < n) {
+          const int p = sb + e;
+          int lo = c0 + 1, hi = L.W - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (st.win[mid] <= p) lo = mid + 1; else hi = mid;
           }
-          unsigned todo = __ballot_sync(mask, zlo <= zhi);
-          while (todo) {
-            const int src = __ffs(todo) - 1;
-            const int lo_r = __shfl_sync(mask, zlo, src);
-            const int hi_r = __shfl_sync(mask, zhi, src);
-            if (!a.accumulate) zero_rows<TC, V, NV>(a, lo_r, hi_r, col0, act, strm);
-            todo &= todo - 1;
+          const int rr = lo - 1;  // window slot of p's row
+          const bool end = st.win[rr + 1] == p + 1;
+          sinfo[e] = (win_base + rr) | (end ? (int)0x80000000 : 0);
+          if (st.win[rr] == p && p != ci.cs) {  // p opens row rr: empties before it start at p too
+            int q = rr - 1;
+            while (q > c0 && st.win[q] == p) q--;
+            zlo = win_base + q + 1;
+            zhi = win_base + rr - 1;
           }
         }
-        __syncwarp(mask);
-      } else {
-        next_start = wget(cur + 1);
-        if (!open) {
-          // the previous row ended at sb: move to the row of the tile's first
-          // nonzero, zeroing the empty rows on the way
-          while (cur < a.M - 1 && next_start <= sb) {
-            cur++;
-            next_start = wget(cur + 1);
-            if (next_start <= sb && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
-          }
+        unsigned todo = __ballot_sync(mask, zlo <= zhi);
+        while (todo) {
+          const int src = __ffs(todo) - 1;
+          const int lo_r = __shfl_sync(mask, zlo, src);
+          const int hi_r = __shfl_sync(mask, zhi, src);
+          if (!a.accumulate) zero_rows<TC, V, NV>(a, lo_r, hi_r, col0, act, strm);
+          todo &= todo - 1;
         }
       }
-    }
-    // ---- consume nonzero e: its B slice has landed in the ring
-    cp_async_wait<SR_R - 1>();
-    float bq[NV][V];
-    ring_read<T, V, NV>(my_ring + (size_t)(e % SR_R) * ring_stride, bq);
-    const T *sval = reinterpret_cast<const T *>(st.val + b * S * L.vs);
-    const float v = ones ? 1.f : Elem<T>::to_f(sval[q]);
-    if (fast) {
-      const int info = st.info[b * S + q];
-      add_row<V, NV, KAHAN>(acc, comp, v, bq);
-      cur = info & 0x7fffffff;
-      open = true;
-      if (info < 0) {
-        flush_done(cur);
-        open = false;
+      __syncwarp(mask);
+      // ---- walk: gather, multiply, store at row ends
+      for (int q = 0; q < n; q += SR_U) {
+        float bv[SR_U][NV][V];
+        #pragma unroll
+        for (int u = 0; u < SR_U; u++) {
+          const int c = q + u < n ? scol[q + u] : -1;
+          const bool live = (unsigned)c < (unsigned)a.K;
+          #pragma unroll
+          for (int j = 0; j < NV; j++) {
+            if (live && act[j]) {
+              load_vec<T, V>(B + (int64_t)c * a.N + col0 + j * V, bv[u][j], keep);
+            } else {
+              #pragma unroll
+              for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+            }
+          }
+        }
+        #pragma unroll
+        for (int u = 0; u < SR_U; u++) {
+          if (q + u >= n) break;
+          const int info = sinfo[q + u];
+          const float v = ones ? 1.f : Elem<T>::to_f(sval[q + u]);
+          add_row<V, NV, KAHAN>(acc, comp, v, bv[u]);
+          cur = info & 0x7fffffff;
+          open = true;
+          if (info < 0) {
+            flush_done(cur);
+            open = false;
+          }
+        }
       }
     } else {
-      const int p = sb + q;
-      if (p >= next_start) {  // the walk left row cur
-        if (open) flush_done(cur);
-        int ns;
-        do {
+      // ---- element by element (tiles crossing long runs of empty rows)
+      int next_start = wget(cur + 1);
+      if (!open) {
+        // the previous row ended at sb: move to the row of the tile's first
+        // nonzero, zeroing the empty rows on the way
+        while (cur < a.M - 1 && next_start <= sb) {
           cur++;
-          ns = wget(cur + 1);
-          if (ns <= p && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
-        } while (ns <= p && cur < a.M - 1);
-        next_start = ns;
+          next_start = wget(cur + 1);
+          if (next_start <= sb && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
+        }
       }
-      add_row<V, NV, KAHAN>(acc, comp, v, bq);
-      open = true;
+      for (int q = 0; q < n; q++) {
+        const int p = sb + q;
+        const int c = scol[q];
+        float bq[NV][V];
+        #pragma unroll
+        for (int j = 0; j < NV; j++) {
+          if ((unsigned)c < (unsigned)a.K && act[j]) {
+            load_vec<T, V>(B + (int64_t)c * a.N + col0 + j * V, bq[j], keep);
+          } else {
+            #pragma unroll
+            for (int i = 0; i < V; i++) bq[j][i] = 0.f;
+          }
+        }
+        if (p >= next_start) {  // the walk left row cur
+          if (open) flush_done(cur);
+          int ns;
+          do {
+            cur++;
+            ns = wget(cur + 1);
+            if (ns <= p && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
+          } while (ns <= p && cur < a.M - 1);
+          next_start = ns;
+        }
+        const float v = ones ? 1.f : Elem<T>::to_f(sval[q]);
+        add_row<V, NV, KAHAN>(acc, comp, v, bq);
+        open = true;
+      }
       // close a row that ends exactly at the tile end; the next tile zeroes
       // any empty rows that follow it
-      if (p == tile_last && next_start == tile_last + 1) {
+      if (next_start == last + 1) {
         flush_done(cur);
         open = false;
       }
     }
-    // ---- the tile is consumed: its buffer takes the tile after next
-    if (e + 1 == nel || q == S - 1) {
-      __syncwarp(mask);
-      if (t + 2 < nst) stage_issue<T, false>(a, st, L, b, sb + 2 * S, min(S, nel - (t + 2) * S), lane, G, mask, strm);
-    }
+    __syncwarp(mask);
+    if (s + 2 < nst)
+      stage_issue<T, false>(a, st, L, b, sb + 2 * L.S, min(L.S, ci.ce - sb - 2 * L.S), lane, G, mask, strm);
   }
-  cp_async_wait<0>();
-  if (!ok) return false;
   // the last row continues past the chunk: head slot or tail slot
   if (open) {
     if (cur == head) {
@@ -459,7 +392,6 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
     }
   }
   if (!a.accumulate && ci.ce >= a.nnz) zero_rows<TC, V, NV>(a, cur + 1, a.M - 1, col0, act, strm);
-  return true;
 }
 
 // ---------------------------------------------------------------------
@@ -558,10 +490,8 @@ __global__ void __launch_bounds__(512, 2) eb_sr_kernel(EbArgs a) {
   const int wib = tid >> a.log2_team_lanes;
   const unsigned wl = tid & 31;
   const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (wl & ~(unsigned)(G - 1)));
-  const int ring_bytes = SEG ? 0 : SR_R * G * V * NV * (int)sizeof(T);
-  const SrLayout L = sr_layout(a.stage, SEG ? 0 : (int)sizeof(T), ring_bytes);
+  const SrLayout L = sr_layout(a.stage, SEG ? 0 : (int)sizeof(T));
   char *g = smem_raw + (size_t)wib * L.bytes;
-  T *ring = reinterpret_cast<T *>(g + L.ring_off);
   Stage st;
   st.bar = reinterpret_cast<uint64_t *>(g);
   st.col = reinterpret_cast<int32_t *>(g + L.col_off);
@@ -588,9 +518,8 @@ __global__ void __launch_bounds__(512, 2) eb_sr_kernel(EbArgs a) {
       if (kahan) sr_seg_chunk<T, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, strm);
       else sr_seg_chunk<T, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, strm);
     } else {
-      const bool ok = kahan ? sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, ring, col0, act, keep, strm)
-                            : sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, ring, col0, act, keep, strm);
-      if (!ok) break;  // a bounded wait expired: copies may still be landing in this group's buffers
+      if (kahan) sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
+      else sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
     }
   }
   // every issued stage was waited for: no bulk copy is in flight here

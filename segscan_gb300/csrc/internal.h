@@ -74,8 +74,7 @@ struct EbGeom {
 
 size_t eb_workspace_bytes(const EbGeom &g, int N);
 // shared memory of the sequential-walk kernels (eb_walk.cu)
-size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes, int ring_bytes);
-int sr_ring_bytes(int G, int V, int NV, int val_bytes);
+size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes);
 
 // Launchers (kernels live in spmm_rb.cu, eb_walk.cu, eb_scan.cu).
 ss_status launch_rbsr(const SpmmCall &c, const RbGeom &g, cudaStream_t s);
