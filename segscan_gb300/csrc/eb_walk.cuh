@@ -31,7 +31,13 @@
 
 namespace ss {
 
-constexpr int SR_U = 4;                       // B rows gathered ahead
+#ifndef SS_SR_GATHER
+#define SS_SR_GATHER 4
+#endif
+#ifndef SS_SR_MIN_BLOCKS
+#define SS_SR_MIN_BLOCKS 2
+#endif
+constexpr int SR_U = SS_SR_GATHER;            // B rows gathered ahead
 constexpr uint32_t SR_SPIN_LIMIT = 1u << 22;  // try_wait polls before giving up
 
 // Per-group shared memory: [bar0 bar1 | col[2][S] | val[2][S] | win[W]]
@@ -482,7 +488,7 @@ __device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lan
 }
 
 template <typename T, typename TC, int V, int NV, bool SEG>
-__global__ void __launch_bounds__(512, 2) eb_sr_kernel(EbArgs a) {
+__global__ void __launch_bounds__(512, SS_SR_MIN_BLOCKS) eb_sr_kernel(EbArgs a) {
   extern __shared__ __align__(16) char smem_raw[];
   const int tid = threadIdx.x;
   const int G = a.team_lanes;
