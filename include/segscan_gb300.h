@@ -246,18 +246,26 @@ ss_status ss_index_validate(const int32_t *index, int nnz, int dst_len,
 /* Batched SpMM: many independent CSR matrices in one persistent launch */
 /* ---------------------------------------------------------------- */
 
-/* A batch plan lives in caller memory: a device table built by
- * ss_batch_plan from host descriptors.  mats/B/C are host arrays of
- * `count` entries holding device pointers.  Per-matrix knobs (may be NULL)
- * choose the row-team shape of each matrix.  Not in the reference. */
+/* A batch plan lives in caller memory: host_bytes of host memory (kept by
+ * the caller and passed to every launch) and dev_bytes of device memory
+ * (256-byte aligned), both sized by ss_batch_plan_size.  mats, B and C are
+ * host arrays of `count` entries (B/C holding device pointers; all
+ * matrices share N and the value dtype).  per_mat[m].thread_nz sets matrix
+ * m's chunk (thread_nz * 2^group_factor nonzeros); group_factor,
+ * coarsen_factor and thread_per_block come from per_mat[0] (NULL = ebsr
+ * defaults).  ss_batch_plan uploads the plan and synchronises the stream.
+ * ss_spmm_batched then computes C[m] = A[m] * B[m] for every m in one
+ * persistent launch plus one fix-up launch, stream-ordered (it can be
+ * replayed from a captured CUDA graph).  Not in the reference. */
 ss_status ss_batch_plan_size(int count, const ss_csr *mats, int N,
-                             size_t *host_bytes, size_t *dev_bytes);
+                             const ss_knobs *per_mat, size_t *host_bytes,
+                             size_t *dev_bytes);
 ss_status ss_batch_plan(int count, const ss_csr *mats, int N,
                         const void *const *B, void *const *C, int c_dtype,
                         const ss_knobs *per_mat, void *host_buf,
                         size_t host_bytes, void *dev_buf, size_t dev_bytes,
                         void *stream);
-ss_status ss_spmm_batched(const void *dev_buf, size_t dev_bytes, void *stream);
+ss_status ss_spmm_batched(const void *host_plan, void *dev_plan, void *stream);
 
 #ifdef __cplusplus
 }

@@ -104,10 +104,11 @@ _SIGNATURES = {
     "ss_sddmm": (c_int, [POINTER(SsCsr), c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "ss_csr_validate": (c_int, [POINTER(SsCsr), c_void_p, c_void_p]),
     "ss_index_validate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p]),
-    "ss_batch_plan_size": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(c_size_t), POINTER(c_size_t)]),
+    "ss_batch_plan_size": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(SsKnobs), POINTER(c_size_t),
+                                   POINTER(c_size_t)]),
     "ss_batch_plan": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(c_void_p), POINTER(c_void_p), c_int,
                               POINTER(SsKnobs), c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
-    "ss_spmm_batched": (c_int, [c_void_p, c_size_t, c_void_p]),
+    "ss_spmm_batched": (c_int, [c_void_p, c_void_p, c_void_p]),
 }
 
 _lib: ctypes.CDLL | None = None

@@ -154,3 +154,49 @@ def best(A: api.CsrMatrix, N: int, B: Optional[torch.Tensor] = None, measure: bo
     for name, v in hit["knobs"].items():
         setattr(k, name, int(v))
     return hit["strategy"], k
+
+
+# ---------------------------------------------------------------------------
+# Batched SpMM: per-matrix chunk sizes
+# ---------------------------------------------------------------------------
+def _lanes_gf(N: int, dtype: torch.dtype) -> int:
+    per_vec = 8 if dtype in (torch.bfloat16, torch.float16) else 4
+    return max(0, min(5, int(math.log2(max(1, N // per_vec)))))
+
+
+def batch_knobs(mats, N: int, target_chunk: int = 512) -> list[SsKnobs]:
+    """Knobs for each matrix of a batch: the walk geometry is shared (group
+    size from N), the chunk (thread_nz * group) is per matrix: at most
+    target_chunk nonzeros, and small enough that a matrix splits into at
+    least four items, so small and skewed matrices still spread over SMs."""
+    out = []
+    for A in mats:
+        dtype = A.dtype
+        gf = _lanes_gf(N, dtype)
+        G = 1 << gf
+        nnz = max(1, A.nnz)
+        chunk = min(target_chunk, max(8 * G, 1 << int(math.ceil(math.log2(max(1, nnz // 4))))))
+        tnz = max(1, chunk // G)
+        out.append(api.make_knobs("ebsr", N, group_factor=gf, coarsen_factor=4, thread_nz=tnz, block_denom=1,
+                                  thread_per_block=256))
+    return out
+
+
+def tune_batch(mats, Bs, N: int, candidates=(256, 512, 1024, 2048), iters: int = 5):
+    """Measures the batched launch for each target chunk; returns
+    (best target, {target: ms})."""
+    from . import batched
+    times = {}
+    for t in candidates:
+        plan = batched.BatchedSpMM(mats, Bs, knobs=batch_knobs(mats, N, t))
+        plan.run()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(iters):
+            plan.run()
+        e1.record(s)
+        e1.synchronize()
+        times[t] = e0.elapsed_time(e1) / iters
+    best = min(times, key=times.get)
+    return best, times

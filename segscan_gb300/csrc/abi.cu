@@ -152,8 +152,8 @@ static void finish_eb(long long worker_cap, EbGeom &g) {
 
 // ebsr: csrspmm_rowcaching_nnzbalance_cg (spmm_cg.cuh:553-566) and
 // segment_coo_sr / _noshmem_sr / _noshmem_lessatom_sr (segscan.cuh:817-829).
-static ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_bytes, const ss_knobs &k,
-                         EbGeom &g) {
+ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_bytes, const ss_knobs &k,
+                  EbGeom &g) {
   ss_status st = check_common_knobs(k);
   if (st) return st;
   if (k.group_factor < 0 || k.group_factor > 5)

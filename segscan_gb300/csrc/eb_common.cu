@@ -50,15 +50,6 @@ EbArgs eb_base_args(const EbGeom &g, void *ws, int N) {
   return a;
 }
 
-__device__ __forceinline__ int lower_bound_idx(const int32_t *index, int n, int key) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (__ldg(index + mid) < key) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
 template <typename TC>
 __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restrict__ rows,
                                                           const float *__restrict__ heads,
@@ -70,37 +61,8 @@ __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restr
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += warps) {
-    const int r = rows[c];
-    if (c == 0 || r < 0 || r >= M) continue;
-    if (rows[c - 1] == r) continue;  // not the leader of this run
-    int cend = c + 1;
-    while (cend < num_chunks && rows[cend] == r) cend++;
-    float count = 1.f;
-    if (reduce == SS_MEAN && index != nullptr) {
-      int lo = 0, hi = 0;
-      if (lane == 0) {
-        lo = lower_bound_idx(index, nnz, r);
-        hi = lower_bound_idx(index, nnz, r + 1);
-      }
-      lo = __shfl_sync(0xffffffffu, lo, 0);
-      hi = __shfl_sync(0xffffffffu, hi, 0);
-      count = (float)max(hi - lo, 1);
-    }
-    TC *crow = C + (int64_t)r * N;
-    for (int j = lane; j < N; j += 32) {
-      float acc = tails[(int64_t)(c - 1) * N + j];  // the owner's partial
-      float comp = 0.f;
-      for (int k = c; k < cend; k++) {
-        const float x = heads[(int64_t)k * N + j];
-        if (reduce == SS_MAX) acc = fmaxf(acc, x);
-        else kahan_add(acc, comp, x);
-      }
-      if (accumulate) acc += Elem<TC>::to_f(crow[j]);
-      if (reduce == SS_MEAN) acc = acc / count;
-      crow[j] = Elem<TC>::from_f(acc);
-    }
-  }
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += warps)
+    fixup_chunk<TC>(rows, heads, tails, num_chunks, N, M, C, reduce, accumulate, index, nnz, c, lane);
 }
 
 ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *C, int c_dtype,

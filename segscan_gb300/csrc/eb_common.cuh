@@ -147,4 +147,53 @@ __device__ __forceinline__ void flush_row(const EbArgs &a, const ChunkInfo &ci, 
   }
 }
 
+__device__ __forceinline__ int lower_bound_idx(const int32_t *index, int n, int key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(index + mid) < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Carry fix-up of chunk c (one warp): when c leads a run of chunks whose
+// head is row r, row r = owner's tail (chunk c - 1) + the run's heads, summed
+// in chunk order with compensation (max for SS_MAX), plus the old output in
+// accumulate mode, divided by the segment length for a mean.
+template <typename TC>
+__device__ __forceinline__ void fixup_chunk(const int32_t *__restrict__ rows, const float *__restrict__ heads,
+                                            const float *__restrict__ tails, int num_chunks, int N, int M, TC *C,
+                                            int reduce, int accumulate, const int32_t *__restrict__ index, int nnz,
+                                            int c, int lane) {
+  const int r = rows[c];
+  if (c == 0 || r < 0 || r >= M) return;
+  if (rows[c - 1] == r) return;  // not the leader of this run
+  int cend = c + 1;
+  while (cend < num_chunks && rows[cend] == r) cend++;
+  float count = 1.f;
+  if (reduce == SS_MEAN && index != nullptr) {
+    int lo = 0, hi = 0;
+    if (lane == 0) {
+      lo = lower_bound_idx(index, nnz, r);
+      hi = lower_bound_idx(index, nnz, r + 1);
+    }
+    lo = __shfl_sync(0xffffffffu, lo, 0);
+    hi = __shfl_sync(0xffffffffu, hi, 0);
+    count = (float)max(hi - lo, 1);
+  }
+  TC *crow = C + (int64_t)r * N;
+  for (int j = lane; j < N; j += 32) {
+    float acc = tails[(int64_t)(c - 1) * N + j];  // the owner's partial
+    float comp = 0.f;
+    for (int k = c; k < cend; k++) {
+      const float x = heads[(int64_t)k * N + j];
+      if (reduce == SS_MAX) acc = fmaxf(acc, x);
+      else kahan_add(acc, comp, x);
+    }
+    if (accumulate) acc += Elem<TC>::to_f(crow[j]);
+    if (reduce == SS_MEAN) acc = acc / count;
+    crow[j] = Elem<TC>::from_f(acc);
+  }
+}
+
 }  // namespace ss

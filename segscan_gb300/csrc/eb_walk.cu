@@ -6,7 +6,7 @@ namespace ss {
 // Device status of the bounded waits; kernels get its address in EbArgs.
 __device__ int g_walk_error;
 
-static int *walk_error_ptr() {
+int *walk_error_ptr() {
   static int *p[64] = {nullptr};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;

@@ -185,8 +185,9 @@ __device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)
   }
 }
 
+// Returns false when a bounded wait expired (the caller then stops).
 template <typename T, typename TC, int V, int NV, bool KAHAN>
-__device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
+__device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
                                               const SrLayout &L, int col0, const bool (&act)[NV], uint64_t keep,
                                               uint64_t strm) {
   const T *__restrict__ B = (const T *)a.B;
@@ -258,7 +259,7 @@ __device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int la
     const int sb = ci.cs + s * L.S;
     const int n = min(L.S, ci.ce - sb);
     const int last = sb + n - 1;
-    if (!stage_wait(st, b, mask, a.err)) return;
+    if (!stage_wait(st, b, mask, a.err)) return false;
     const int32_t *scol = st.col + b * L.S;
     const T *sval = reinterpret_cast<const T *>(st.val + b * L.S * L.vs);
     int32_t *sinfo = st.info + b * L.S;
@@ -398,6 +399,7 @@ __device__ __forceinline__ void sr_spmm_chunk(const EbArgs &a, int chunk, int la
     }
   }
   if (!a.accumulate && ci.ce >= a.nnz) zero_rows<TC, V, NV>(a, cur + 1, a.M - 1, col0, act, strm);
+  return true;
 }
 
 // ---------------------------------------------------------------------
@@ -524,8 +526,9 @@ __global__ void __launch_bounds__(512, SS_SR_MIN_BLOCKS) eb_sr_kernel(EbArgs a) 
       if (kahan) sr_seg_chunk<T, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, strm);
       else sr_seg_chunk<T, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, strm);
     } else {
-      if (kahan) sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
-      else sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
+      const bool ok = kahan ? sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm)
+                            : sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
+      if (!ok) break;  // a bounded wait expired: copies may still be landing in this group's buffers
     }
   }
   // every issued stage was waited for: no bulk copy is in flight here

@@ -73,8 +73,13 @@ struct EbGeom {
 };
 
 size_t eb_workspace_bytes(const EbGeom &g, int N);
+// Sequential-walk geometry from knobs (abi.cu): worker_units scales
+// block_factor (nrow for SpMM, nnz for segments); val_bytes 0 for segments.
+ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_bytes, const ss_knobs &k, EbGeom &g);
 // shared memory of the sequential-walk kernels (eb_walk.cu)
 size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes);
+// device address of the bounded-wait status word (eb_walk.cu)
+int *walk_error_ptr();
 
 // Launchers (kernels live in spmm_rb.cu, eb_walk.cu, eb_scan.cu).
 ss_status launch_rbsr(const SpmmCall &c, const RbGeom &g, cudaStream_t s);
