@@ -174,10 +174,13 @@ def batch_knobs(mats, N: int, target_chunk: int = 512) -> list[SsKnobs]:
         dtype = A.dtype
         gf = _lanes_gf(N, dtype)
         G = 1 << gf
+        vec = 8 if dtype in (torch.bfloat16, torch.float16) else 4
+        while vec > 1 and N % vec:
+            vec //= 2  # one vector per lane: the widest that divides N
         nnz = max(1, A.nnz)
         chunk = min(target_chunk, max(8 * G, 1 << int(math.ceil(math.log2(max(1, nnz // 4))))))
         tnz = max(1, chunk // G)
-        out.append(api.make_knobs("ebsr", N, group_factor=gf, coarsen_factor=4, thread_nz=tnz, block_denom=1,
+        out.append(api.make_knobs("ebsr", N, group_factor=gf, coarsen_factor=vec, thread_nz=tnz, block_denom=1,
                                   thread_per_block=256))
     return out
 
