@@ -46,6 +46,9 @@ def parse():
                     help="knob overrides for --strategy: JSON or name=value:name=value")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--extras", dest="extras", action="store_true", default=True,
+                    help="also measure BF16/FP16 precision, the 512-matrix batch and fwd+bwd (default)")
+    ap.add_argument("--no-extras", dest="extras", action="store_false")
     return ap.parse_args()
 
 
@@ -227,6 +230,135 @@ def choose(args, A_dev, N):
     return autotune.best(A_dev, N)
 
 
+def _event_ms(fn, iters, stream, warm=2):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(iters):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / iters
+
+
+def _errors(C, C64, absC):
+    import numpy as np
+    err = np.abs(C.astype(np.float64) - C64)
+    return {"normwise_rel": float(np.linalg.norm(err) / max(np.linalg.norm(C64), 1e-300)),
+            "max_rel_to_sum_abs": float((err / np.maximum(absC, 1e-300)).max()),
+            "max_abs_over_max_ref": float(err.max() / max(np.abs(C64).max(), 1e-300))}
+
+
+def extra_precision(A, B, N, fp32_ms, dev):
+    """BF16 / FP16 storage of A.vals and B, FP32 accumulation (Kahan on rows
+    above 1024 nonzeros), on the power-law matrix: throughput beside plain
+    FP32, and error against FP64 on the FP32 inputs."""
+    import torch
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_lib
+    from segscan_gb300 import api, autotune, synth
+    C64, absC = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B)
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    for name, dt, cdt in (("bf16_c_f32", torch.bfloat16, torch.float32), ("bf16_c_bf16", torch.bfloat16, torch.bfloat16),
+                          ("f16_c_f32", torch.float16, torch.float32)):
+        Ad = api.CsrMatrix.from_host(A, dev, dt)
+        Bd = torch.from_numpy(B).to(dev).to(dt)
+        strategy, k = autotune.best(Ad, N, Bd)
+        Cd = torch.empty((A.nrow, N), dtype=cdt, device=dev)
+        wsz = api.spmm_workspace_size(Ad, N, strategy, k)
+        ws = torch.empty(wsz + 256, dtype=torch.uint8, device=dev) if wsz else None
+        ms = _event_ms(lambda: api.spmm(Ad, Bd, strategy, knobs=k, out=Cd, workspace=ws), 20, stream)
+        nb = synth.spmm_bytes(A, N, val_bytes=2, b_bytes=2, c_bytes=2 if cdt != torch.float32 else 4)
+        out[name] = {"ms": ms, "GB/s": nb / ms / 1e6, "speedup_vs_fp32": fp32_ms / ms, "strategy": strategy,
+                     "knobs": k.as_dict(), **_errors(Cd.float().cpu().numpy(), C64, absC)}
+    out["tolerance"] = "normwise <= 2e-2 vs FP64 on FP32 inputs"
+    return out
+
+
+def extra_batched(dev, N=64, count=512):
+    """512 CSR matrices (rows log-uniform in [100, 50000], row length Zipf 2.3
+    clipped to [1, 2000], seed 3): one persistent launch replayed from a CUDA
+    graph (BF16 storage, FP32 accumulation) against one plain FP32 launch per
+    matrix."""
+    import numpy as np
+    import torch
+    from segscan_gb300 import api, autotune, batched, synth
+    mats_h = synth.batch(count, 100, 50_000, 2.3, 2000, seed=3)
+    rng = np.random.default_rng(33)
+    Bh = [(rng.random((A.ncol, N), dtype=np.float32) * 2 - 1) for A in mats_h]
+    stream = torch.cuda.current_stream(dev)
+    res = {"matrices": count, "rows": int(sum(A.nrow for A in mats_h)), "nnz": int(sum(A.nnz for A in mats_h))}
+    mats32 = [api.CsrMatrix.from_host(A, dev) for A in mats_h]
+    B32 = [torch.from_numpy(b).to(dev) for b in Bh]
+    knobs32 = autotune.batch_knobs(mats32, N)
+    outs = [torch.empty((A.nrow, N), device=dev) for A in mats_h]
+    wss = []
+    for A, k in zip(mats32, knobs32):
+        n = api.spmm_workspace_size(A, N, "ebsr", k)
+        wss.append(torch.empty(n + 256, dtype=torch.uint8, device=dev) if n else None)
+    plain_ms = _event_ms(lambda: batched.plain_per_matrix(mats32, B32, outs, [("ebsr", k) for k in knobs32], wss), 3,
+                         stream, warm=1)
+    res["plain_fp32_per_matrix_ms"] = plain_ms
+    for name, dt, cdt in (("batched_fp32_graph", torch.float32, torch.float32),
+                          ("batched_bf16_graph", torch.bfloat16, torch.bfloat16),
+                          ("batched_bf16_c_f32_graph", torch.bfloat16, torch.float32)):
+        mats = [api.CsrMatrix.from_host(A, dev, dt) for A in mats_h]
+        Bs = [b.to(dt) for b in B32]
+        target, tried = autotune.tune_batch(mats, Bs, N)
+        plan = batched.BatchedSpMM(mats, Bs, out_dtype=cdt, knobs=autotune.batch_knobs(mats, N, target))
+        plan.capture()
+        ms = _event_ms(plan.replay, 10, stream)
+        err = []
+        for i in range(0, count, 64):  # spot-check a few matrices against FP32 per-matrix results
+            ref = outs[i].double()
+            err.append(float((plan.out[i].double() - ref).norm() / max(float(ref.norm()), 1e-300)))
+        res[name] = {"ms": ms, "speedup_vs_plain_fp32": plain_ms / ms, "chunk_target": target,
+                     "max_normwise_rel_vs_fp32": max(err)}
+    return res
+
+
+def extra_fwd_bwd(dev, N=128):
+    """Differentiated SpMM layer: power-law 2e6 x 2e6 (Zipf 2.1 clipped to
+    [1, 50000], seed 4), B 2e6 x 128, dC ~ N(0, 1).  Forward C = A B;
+    backward dA.vals = SDDMM(dC, B), dB = A^T dC on the device-built
+    transpose (built once per pattern; its time is reported apart)."""
+    import numpy as np
+    import torch
+    from segscan_gb300 import api, autograd, synth
+    A = synth.powerlaw(2_000_000, 2_000_000, 2.1, 1, 50_000, seed=4)
+    stream = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(4)
+    dC = torch.from_numpy(rng.standard_normal((A.nrow, N), dtype=np.float32)).to(dev)
+    B32 = torch.from_numpy(synth.dense(A.ncol, N, seed=44)).to(dev)
+    res = {"nrow": A.nrow, "nnz": A.nnz, "N": N}
+    knobs = api.make_knobs("ebsr", N, group_factor=5, thread_nz=32, thread_per_block=512, block_denom=1)
+    for name, dt in (("fp32", torch.float32), ("bf16", torch.bfloat16)):
+        Ad = api.CsrMatrix.from_host(A, dev, dt, values=False)
+        vals = torch.from_numpy(A.values).to(dev).to(dt).requires_grad_(True)
+        Bd = B32.to(dt).requires_grad_(True)
+        pat = autograd.pattern(Ad)
+        t_ms = _event_ms(lambda: api.transpose(Ad), 3, stream, warm=1)
+        pat.transposed()
+
+        def step():
+            vals.grad = None
+            Bd.grad = None
+            C = autograd.spmm(Ad, vals, Bd, "ebsr", knobs, "ebsr", pattern=pat)
+            C.backward(dC)
+
+        def fwd():
+            autograd.spmm(Ad, vals.detach(), Bd.detach(), "ebsr", knobs, pattern=pat)
+
+        total = _event_ms(step, 5, stream)
+        f = _event_ms(fwd, 5, stream)
+        res[name] = {"fwd_bwd_ms": total, "fwd_ms": f, "bwd_ms": total - f, "transpose_build_ms": t_ms}
+    return res
+
+
 def run_ours(args):
     import torch
     from segscan_gb300 import api, synth
@@ -281,37 +413,51 @@ def run_ours(args):
         t = float(tt.item())
 
     # end to end through the public API: host inputs in pinned memory,
-    # H2D of A and B, the SpMM, D2H of C, every step
+    # H2D of A and B, the SpMM, D2H of C, every step; consecutive steps
+    # alternate between two streams and buffer sets, so one step's copies
+    # overlap the next step's (each step still moves all of its own bytes)
     h_indptr = torch.from_numpy(A.indptr).pin_memory()
     h_indices = torch.from_numpy(A.indices).pin_memory()
     h_values = torch.from_numpy(A.values).pin_memory()
     h_B = torch.from_numpy(B).pin_memory()
-    h_C = torch.empty((A.nrow, N), dtype=torch.float32).pin_memory()
-    d_indptr = torch.empty_like(Ad.indptr)
-    d_indices = torch.empty_like(Ad.indices)
-    d_values = torch.empty_like(Ad.values)
-    d_B = torch.empty_like(Bd)
-    Ae = api.CsrMatrix(A.nrow, A.ncol, d_indptr, d_indices, d_values)
+    e2e_streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    sets = []
+    for _ in range(2):
+        d = dict(indptr=torch.empty_like(Ad.indptr), indices=torch.empty_like(Ad.indices),
+                 values=torch.empty_like(Ad.values), B=torch.empty_like(Bd), C=torch.empty_like(C),
+                 hC=torch.empty((A.nrow, N), dtype=torch.float32).pin_memory(),
+                 ws=torch.empty_like(work) if work is not None else None)
+        d["A"] = api.CsrMatrix(A.nrow, A.ncol, d["indptr"], d["indices"], d["values"])
+        sets.append(d)
     h2d = sum(x.numel() * x.element_size() for x in (h_indptr, h_indices, h_values, h_B))
-    d2h = h_C.numel() * h_C.element_size()
+    d2h = sets[0]["hC"].numel() * sets[0]["hC"].element_size()
 
-    def e2e_step():
-        d_indptr.copy_(h_indptr, non_blocking=True)
-        d_indices.copy_(h_indices, non_blocking=True)
-        d_values.copy_(h_values, non_blocking=True)
-        d_B.copy_(h_B, non_blocking=True)
-        api.spmm(Ae, d_B, strategy, knobs=knobs, out=C, workspace=work, stream=stream)
-        h_C.copy_(C, non_blocking=True)
+    def e2e_step(i):
+        s_ = e2e_streams[i % 2]
+        d = sets[i % 2]
+        with torch.cuda.stream(s_):
+            d["indptr"].copy_(h_indptr, non_blocking=True)
+            d["indices"].copy_(h_indices, non_blocking=True)
+            d["values"].copy_(h_values, non_blocking=True)
+            d["B"].copy_(h_B, non_blocking=True)
+            api.spmm(d["A"], d["B"], strategy, knobs=knobs, out=d["C"], workspace=d["ws"], stream=s_)
+            d["hC"].copy_(d["C"], non_blocking=True)
+
+    def e2e_run(k):
+        for s_ in e2e_streams:
+            s_.wait_stream(stream)
+        for i in range(k):
+            e2e_step(i)
+        for s_ in e2e_streams:
+            stream.wait_stream(s_)
 
     t_e2e = float("nan")
     if args.e2e_steps > 0:
-        for _ in range(2):
-            e2e_step()
+        e2e_run(2)
         torch.cuda.synchronize(dev)
         barrier()
         e0.record(stream)
-        for _ in range(args.e2e_steps):
-            e2e_step()
+        e2e_run(args.e2e_steps)
         e1.record(stream)
         torch.cuda.synchronize(dev)
         t_e2e = e0.elapsed_time(e1) / 1e3 / args.e2e_steps
@@ -343,6 +489,17 @@ def run_ours(args):
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clocks,
     }
+    if ws_ == 1 and args.extras:
+        configs = {}
+        for key, fn in (("precision_powerlaw_n64", lambda: extra_precision(A, B, N, t * 1e3, dev)),
+                        ("batched_512", lambda: extra_batched(dev)),
+                        ("fwd_bwd_powerlaw_2e6_n128", lambda: extra_fwd_bwd(dev))):
+            try:
+                configs[key] = fn()
+            except Exception as exc:  # report, never hide, a failing extra measurement
+                configs[key] = {"error": f"{type(exc).__name__}: {exc}"}
+            torch.cuda.empty_cache()
+        line["configs"] = configs
     if ws_ == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample, desc, _ = cpu_sample(A, B, 2.0, threads)
