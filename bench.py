@@ -347,7 +347,7 @@ def extra_fwd_bwd(dev, N=128):
         def step():
             vals.grad = None
             Bd.grad = None
-            C = autograd.spmm(Ad, vals, Bd, "ebsr", knobs, "ebsr", pattern=pat)
+            C = autograd.spmm(Ad, vals, Bd, "ebsr", knobs, "ebsr", pattern=pat, bw_knobs=knobs)
             C.backward(dC)
 
         def fwd():

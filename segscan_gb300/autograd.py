@@ -36,12 +36,13 @@ class _Pattern:
 
 class SpMMFunction(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, values, B, pattern: _Pattern, strategy: str, knobs, bw_strategy: str):
+    def forward(ctx, values, B, pattern: _Pattern, strategy: str, knobs, bw_strategy: str, bw_knobs):
         A = pattern.A.with_values(values.contiguous())
         C = api.spmm(A, B.contiguous(), strategy, knobs=knobs)
         ctx.save_for_backward(values, B)
         ctx.pattern = pattern
         ctx.bw_strategy = bw_strategy
+        ctx.bw_knobs = bw_knobs
         return C
 
     @staticmethod
@@ -56,15 +57,16 @@ class SpMMFunction(torch.autograd.Function):
         if ctx.needs_input_grad[1]:
             AT, perm = pattern.transposed()
             t_vals = api.gather_values(values.float().contiguous(), perm)
-            d_B = api.spmm(AT.with_values(t_vals), dC, ctx.bw_strategy).to(B.dtype)
-        return d_values, d_B, None, None, None, None
+            d_B = api.spmm(AT.with_values(t_vals), dC, ctx.bw_strategy, knobs=ctx.bw_knobs).to(B.dtype)
+        return d_values, d_B, None, None, None, None, None
 
 
 def spmm(A: api.CsrMatrix, values: torch.Tensor, B: torch.Tensor, strategy: str = "ebsr", knobs=None,
-         bw_strategy: str = "ebsr", pattern: Optional[_Pattern] = None) -> torch.Tensor:
-    """C = A(values) @ B, differentiable in values and B."""
+         bw_strategy: str = "ebsr", pattern: Optional[_Pattern] = None, bw_knobs=None) -> torch.Tensor:
+    """C = A(values) @ B, differentiable in values and B (bw_* choose the
+    strategy and knobs of the backward's A^T @ dC)."""
     pattern = pattern or _Pattern(A)
-    return SpMMFunction.apply(values, B, pattern, strategy, knobs, bw_strategy)
+    return SpMMFunction.apply(values, B, pattern, strategy, knobs, bw_strategy, bw_knobs)
 
 
 def pattern(A: api.CsrMatrix) -> _Pattern:
