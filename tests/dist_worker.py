@@ -1,0 +1,32 @@
+"""Rank body for the world-size-2 gloo tests of segscan_gb300.partition
+(spawned processes; CPU only)."""
+import os
+
+import numpy as np
+import torch
+import torch.distributed as dist
+
+
+def run(rank: int, world: int, port: int, out_dir: str) -> None:
+    import oracle_lib
+    from segscan_gb300 import partition, synth
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        csr = synth.powerlaw(3000, 2500, 2.1, 1, 400, seed=17)
+        N = 8
+        B = synth.dense(csr.ncol, N, seed=18)
+        dC = synth.dense(csr.nrow, N, seed=19)
+        blocks = partition.row_blocks(csr.indptr, world)
+        part, (r0, r1) = partition.local_shard(csr, rank, world)
+        # forward: this rank's rows with the reference's check-path loop
+        C_local = oracle_lib.spmm_check_f32(part.indptr, part.indices, part.values, B)
+        C = partition.gather_rows(torch.from_numpy(C_local), blocks)
+        # backward: partial dB = A_block^T dC_block in FP64, then one all-reduce
+        t_indptr, t_indices, perm = oracle_lib.csr_transpose(part.indptr, part.indices, part.ncol)
+        dB_part, _ = oracle_lib.spmm_f64(t_indptr, t_indices, part.values[perm], dC[r0:r1])
+        dB = partition.reduce_dB(torch.from_numpy(dB_part))
+        if rank == 0:
+            np.save(os.path.join(out_dir, "C.npy"), C.numpy())
+            np.save(os.path.join(out_dir, "dB.npy"), dB.numpy())
+    finally:
+        dist.destroy_process_group()

@@ -1,0 +1,83 @@
+"""Row-block sharding (segscan_gb300.partition): balance and coverage, and a
+world-size-2 gloo run (CPU) whose gathered C and all-reduced dB equal the
+unsharded results."""
+import socket
+
+import numpy as np
+import pytest
+import torch
+
+import oracle_lib
+from segscan_gb300 import partition, synth
+
+
+def test_row_blocks_cover_and_balance():
+    csr = synth.powerlaw(50000, 50000, 2.1, 1, 5000, seed=2)
+    L = csr.row_lengths()
+    for parts in (1, 2, 3, 8, 17):
+        blocks = partition.row_blocks(csr.indptr, parts)
+        assert blocks[0][0] == 0 and blocks[-1][1] == csr.nrow
+        assert all(b[1] == c[0] for b, c in zip(blocks, blocks[1:]))
+        sizes = [int(csr.indptr[r1] - csr.indptr[r0]) for r0, r1 in blocks]
+        assert sum(sizes) == csr.nnz
+        assert max(sizes) - csr.nnz / parts <= L.max()  # off by less than one row
+
+
+def test_row_blocks_edge_cases():
+    empty = np.zeros(11, np.int32)  # 10 rows, no nonzeros
+    assert sum(r1 - r0 for r0, r1 in partition.row_blocks(empty, 3)) == 10
+    one_row = np.array([0, 1000], np.int32)
+    blocks = partition.row_blocks(one_row, 4)
+    assert sum(r1 - r0 for r0, r1 in blocks) == 1
+    few = np.array([0, 1, 2], np.int32)
+    assert sum(r1 - r0 for r0, r1 in partition.row_blocks(few, 5)) == 2
+
+
+def test_shards_reassemble_on_cpu():
+    csr = synth.poisson(2000, 1500, 6.0, seed=3)
+    B = synth.dense(1500, 4, seed=4)
+    full = oracle_lib.spmm_check_f32(csr.indptr, csr.indices, csr.values, B)
+    parts = [partition.shard(csr, r0, r1) for r0, r1 in partition.row_blocks(csr.indptr, 3)]
+    got = np.concatenate([oracle_lib.spmm_check_f32(p.indptr, p.indices, p.values, B) for p in parts])
+    assert np.array_equal(got.view(np.uint32), full.view(np.uint32))  # rows are independent: same bits
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_gloo_world2_forward_and_backward(tmp_path):
+    import dist_worker
+    torch.multiprocessing.start_processes(dist_worker.run, args=(2, free_port(), str(tmp_path)), nprocs=2,
+                                          join=True, start_method="spawn")
+    csr = synth.powerlaw(3000, 2500, 2.1, 1, 400, seed=17)
+    B = synth.dense(csr.ncol, 8, seed=18)
+    dC = synth.dense(csr.nrow, 8, seed=19)
+    full = oracle_lib.spmm_check_f32(csr.indptr, csr.indices, csr.values, B)
+    C = np.load(tmp_path / "C.npy")
+    assert np.array_equal(C.view(np.uint32), full.view(np.uint32))
+    t_indptr, t_indices, perm = oracle_lib.csr_transpose(csr.indptr, csr.indices, csr.ncol)
+    dB_full, dB_abs = oracle_lib.spmm_f64(t_indptr, t_indices, csr.values[perm], dC)
+    dB = np.load(tmp_path / "dB.npy")
+    assert np.all(np.abs(dB - dB_full) <= 1e-12 * dB_abs + 1e-300)
+
+
+@pytest.mark.gpu
+def test_gpu_shards_reassemble(cuda):
+    from gpu_util import check_close, dev_csr, oracle64
+    from segscan_gb300 import api
+    csr = synth.powerlaw(40000, 40000, 2.1, 1, 5000, seed=21)
+    N = 64
+    B = synth.dense(csr.ncol, N, seed=22)
+    Bd = torch.from_numpy(B).cuda()
+    C64, absC = oracle64(csr, B)
+    for strategy in ("ebsr", "rbsr"):
+        full = api.spmm(dev_csr(csr), Bd, strategy).cpu().numpy()
+        parts = [api.spmm(dev_csr(partition.shard(csr, r0, r1)), Bd, strategy).cpu().numpy()
+                 for r0, r1 in partition.row_blocks(csr.indptr, 4)]
+        got = np.concatenate(parts)
+        check_close(got, C64, absC, 1e-5, 1e-5, f"{strategy} shards")
+        if strategy == "rbsr":  # a row's arithmetic does not depend on the sharding
+            assert np.array_equal(got.view(np.uint32), full.view(np.uint32))
