@@ -300,9 +300,17 @@ def extra_batched(dev, N=64, count=512):
     for A, k in zip(mats32, knobs32):
         n = api.spmm_workspace_size(A, N, "ebsr", k)
         wss.append(torch.empty(n + 256, dtype=torch.uint8, device=dev) if n else None)
-    plain_ms = _event_ms(lambda: batched.plain_per_matrix(mats32, B32, outs, [("ebsr", k) for k in knobs32], wss), 3,
-                         stream, warm=1)
+    plain = lambda: batched.plain_per_matrix(mats32, B32, outs, [("ebsr", k) for k in knobs32], wss)
+    plain_ms = _event_ms(plain, 3, stream, warm=1)
     res["plain_fp32_per_matrix_ms"] = plain_ms
+    # the same per-matrix launches replayed from one CUDA graph (no host
+    # overhead left: what remains is one walk + one fix-up launch per matrix)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plain()
+    plain_graph_ms = _event_ms(g.replay, 5, stream)
+    res["plain_fp32_per_matrix_graph_ms"] = plain_graph_ms
+    del g
     for name, dt, cdt in (("batched_fp32_graph", torch.float32, torch.float32),
                           ("batched_bf16_graph", torch.bfloat16, torch.bfloat16),
                           ("batched_bf16_c_f32_graph", torch.bfloat16, torch.float32)):
@@ -316,7 +324,8 @@ def extra_batched(dev, N=64, count=512):
         for i in range(0, count, 64):  # spot-check a few matrices against FP32 per-matrix results
             ref = outs[i].double()
             err.append(float((plan.out[i].double() - ref).norm() / max(float(ref.norm()), 1e-300)))
-        res[name] = {"ms": ms, "speedup_vs_plain_fp32": plain_ms / ms, "chunk_target": target,
+        res[name] = {"ms": ms, "speedup_vs_plain_fp32": plain_ms / ms,
+                     "speedup_vs_plain_fp32_graph": plain_graph_ms / ms, "chunk_target": target,
                      "max_normwise_rel_vs_fp32": max(err)}
     return res
 
@@ -335,8 +344,12 @@ def extra_fwd_bwd(dev, N=128):
     dC = torch.from_numpy(rng.standard_normal((A.nrow, N), dtype=np.float32)).to(dev)
     B32 = torch.from_numpy(synth.dense(A.ncol, N, seed=44)).to(dev)
     res = {"nrow": A.nrow, "nnz": A.nnz, "N": N}
-    knobs = api.make_knobs("ebsr", N, group_factor=5, thread_nz=32, thread_per_block=512, block_denom=1)
+    # one B row per group: 32 lanes x 4 FP32, or 16 lanes x 8 BF16 (16 bytes per lane either way)
+    knobs32 = api.make_knobs("ebsr", N, group_factor=5, thread_nz=32, thread_per_block=512, block_denom=1)
+    knobs16 = api.make_knobs("ebsr", N, group_factor=4, coarsen_factor=8, thread_nz=32, thread_per_block=512,
+                             block_denom=1)
     for name, dt in (("fp32", torch.float32), ("bf16", torch.bfloat16)):
+        knobs = knobs32 if dt == torch.float32 else knobs16
         Ad = api.CsrMatrix.from_host(A, dev, dt, values=False)
         vals = torch.from_numpy(A.values).to(dev).to(dt).requires_grad_(True)
         Bd = B32.to(dt).requires_grad_(True)
@@ -347,7 +360,7 @@ def extra_fwd_bwd(dev, N=128):
         def step():
             vals.grad = None
             Bd.grad = None
-            C = autograd.spmm(Ad, vals, Bd, "ebsr", knobs, "ebsr", pattern=pat, bw_knobs=knobs)
+            C = autograd.spmm(Ad, vals, Bd, "ebsr", knobs, "ebsr", pattern=pat, bw_knobs=knobs32)
             C.backward(dC)
 
         def fwd():
@@ -355,7 +368,15 @@ def extra_fwd_bwd(dev, N=128):
 
         total = _event_ms(step, 5, stream)
         f = _event_ms(fwd, 5, stream)
-        res[name] = {"fwd_bwd_ms": total, "fwd_ms": f, "bwd_ms": total - f, "transpose_build_ms": t_ms}
+        # the backward's pieces, timed alone
+        A_v = Ad.with_values(vals.detach())
+        sd = _event_ms(lambda: api.sddmm(A_v, dC, Bd.detach()), 5, stream)
+        AT, perm = pat.transposed()
+        AT_v = AT.with_values(api.gather_values(vals.detach().float(), perm))
+        dB = torch.empty((A.ncol, N), device=dev)
+        db = _event_ms(lambda: api.spmm(AT_v, dC, "ebsr", knobs=knobs32, out=dB), 5, stream)
+        res[name] = {"fwd_bwd_ms": total, "fwd_ms": f, "bwd_ms": total - f, "sddmm_ms": sd, "dB_spmm_ms": db,
+                     "transpose_build_ms": t_ms, "knobs_fwd": knobs.as_dict()}
     return res
 
 
@@ -461,6 +482,36 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         t_e2e = e0.elapsed_time(e1) / 1e3 / args.e2e_steps
+    # link diagnostics for the e2e number: pinned-copy GB/s one way, and both
+    # ways at once on two streams
+    copy_gbs = {}
+    if args.e2e_steps > 0:
+        d0, d1 = sets[0], sets[1]
+
+        def timed(fn, nbytes_, reps=5):
+            fn()
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            return nbytes_ * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+        def both():
+            for s_ in e2e_streams:
+                s_.wait_stream(stream)
+            with torch.cuda.stream(e2e_streams[0]):
+                d0["B"].copy_(h_B, non_blocking=True)
+            with torch.cuda.stream(e2e_streams[1]):
+                d1["hC"].copy_(d1["C"], non_blocking=True)
+            for s_ in e2e_streams:
+                stream.wait_stream(s_)
+
+        nb_B, nb_C = h_B.numel() * 4, d2h
+        copy_gbs = {"h2d": timed(lambda: d0["B"].copy_(h_B, non_blocking=True), nb_B),
+                    "d2h": timed(lambda: d0["hC"].copy_(d0["C"], non_blocking=True), nb_C),
+                    "h2d_plus_d2h_concurrent": timed(both, nb_B + nb_C)}
     if ws_ > 1:
         import torch.distributed as dist
         tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
@@ -485,7 +536,7 @@ def run_ours(args):
                      "kernel": f"{strategy} SpMM step (main kernel + carry fix-up)",
                      "bytes_per_launch": nbytes},
         "e2e": {"value": nbytes / t_e2e / 1e9 * ws_, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
+                "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3, "pinned_copy_gbs": copy_gbs},
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clocks,
     }

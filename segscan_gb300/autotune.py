@@ -52,31 +52,35 @@ def signature(A: api.CsrMatrix, N: int, f: Optional[dict] = None) -> str:
     return f"M{lg(f['M'])}_nnz{lg(f['nnz'])}_mean{lg(f['mean'] + 1)}_max{lg(f['max'] + 1)}_cv{cvb}_N{N}_{A.dtype}"
 
 
-def candidates(N: int) -> list[tuple[str, dict]]:
+def candidates(N: int, dtype: torch.dtype = torch.float32) -> list[tuple[str, dict]]:
     """Strategy / knob candidates (README best static tuples, params.md grids,
-    and longer ebsr chunks, which suit the carry design)."""
+    and longer ebsr chunks, which suit the carry design).  16-bit storage also
+    tries 8-element vectors (16 bytes per lane, half the lanes per B row)."""
     c: list[tuple[str, dict]] = []
     for gf, denom in ((5, 8), (5, 16), (4, 4)):
         c.append(("ebpr", dict(group_factor=gf, tile_factor=5, block_denom=denom)))
     for gf, tf, denom in ((3, 3, 2), (2, 2, 1), (4, 4, 2)):
         c.append(("rbpr", dict(group_factor=gf, tile_factor=tf, block_denom=denom)))
-    lanes_gf = max(0, min(5, int(math.log2(max(1, N // 4)))))
-    for gf in sorted({lanes_gf, max(0, lanes_gf - 1)}):
-        for tnz in (2, 4, 8, 16, 32, 64):
-            for tpb in (128, 256, 512):
-                c.append(("ebsr", dict(group_factor=gf, coarsen_factor=4, thread_nz=tnz, block_denom=1,
-                                       thread_per_block=tpb)))
+    vecs = (8, 4) if dtype in (torch.bfloat16, torch.float16) else (4,)
+    for vec in vecs:
+        lanes_gf = max(0, min(5, int(math.log2(max(1, N // vec)))))
+        for gf in sorted({lanes_gf, max(0, lanes_gf - 1)}):
+            for tnz in (2, 4, 8, 16, 32, 64):
+                for tpb in (128, 256, 512):
+                    c.append(("ebsr", dict(group_factor=gf, coarsen_factor=vec, thread_nz=tnz, block_denom=1,
+                                           thread_per_block=tpb)))
     for cf, tf in ((4, 5), (4, 6), (2, 5)):
         c.append(("rbsr", dict(coarsen_factor=cf, tile_factor=tf)))
     return c
 
 
-def heuristic(f: dict, N: int) -> tuple[str, dict]:
+def heuristic(f: dict, N: int, dtype: torch.dtype = torch.float32) -> tuple[str, dict]:
     """Choice without measuring: element-balanced sequential for skewed rows,
     row-balanced sequential for short regular rows."""
-    lanes_gf = max(0, min(5, int(math.log2(max(1, N // 4)))))
+    vec = 8 if dtype in (torch.bfloat16, torch.float16) and N % 8 == 0 else 4
+    lanes_gf = max(0, min(5, int(math.log2(max(1, N // vec)))))
     if f["cv"] > 1.0 or f["max"] > 256:
-        return "ebsr", dict(group_factor=lanes_gf, coarsen_factor=4, thread_nz=8, block_denom=1)
+        return "ebsr", dict(group_factor=lanes_gf, coarsen_factor=vec, thread_nz=8, block_denom=1)
     return "rbsr", dict(coarsen_factor=4, tile_factor=max(0, min(7, int(math.log2(max(1, N))))))
 
 
@@ -121,7 +125,7 @@ def tune(A: api.CsrMatrix, N: int, B: Optional[torch.Tensor] = None, iters: int 
     if B is None:
         B = torch.rand((A.ncol, N), device=A.indptr.device, dtype=torch.float32).to(A.dtype)
     res = []
-    for strategy, kw in candidates(N):
+    for strategy, kw in candidates(N, A.dtype):
         try:
             k = api.make_knobs(strategy, N, **kw)
             ms = time_candidate(A, B, strategy, k, iters)
@@ -144,7 +148,7 @@ def best(A: api.CsrMatrix, N: int, B: Optional[torch.Tensor] = None, measure: bo
             strategy, kw = ranked[0][1], ranked[0][2]
             hit = {"strategy": strategy, "knobs": kw, "ms": ranked[0][0]}
         else:
-            strategy, kw = heuristic(f, N)
+            strategy, kw = heuristic(f, N, A.dtype)
             hit = {"strategy": strategy, "knobs": api.make_knobs(strategy, N, **kw).as_dict()}
         with _LOCK:
             _MEM[key] = hit

@@ -37,6 +37,16 @@ namespace ss {
 #ifndef SS_SR_MIN_BLOCKS
 #define SS_SR_MIN_BLOCKS 2
 #endif
+// L2 prefetch of B rows SS_SR_PF_DIST nonzeros ahead of the gathers:
+// mode 1 = every lane prefetches its own slice (prefetch.global.L2),
+// mode 2 = one lane per row prefetches the group's whole slice of the row
+// (cp.async.bulk.prefetch.L2); 0 = off
+#ifndef SS_SR_PF_MODE
+#define SS_SR_PF_MODE 0
+#endif
+#ifndef SS_SR_PF_DIST
+#define SS_SR_PF_DIST 16
+#endif
 constexpr int SR_U = SS_SR_GATHER;            // B rows gathered ahead
 constexpr uint32_t SR_SPIN_LIMIT = 1u << 22;  // try_wait polls before giving up
 
@@ -185,6 +195,21 @@ __device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)
   }
 }
 
+// Prefetches into L2 the B row of staged nonzero column c (mode 1: this
+// lane's slice; mode 2: the group's slice, issued by one lane).
+template <typename T, int V, int NV>
+__device__ __forceinline__ void sr_prefetch_row(const EbArgs &a, const T *B, int c, int col0, const bool (&act)[NV],
+                                                int tile_col0, uint32_t tile_bytes) {
+  if ((unsigned)c >= (unsigned)a.K) return;
+  if constexpr (SS_SR_PF_MODE == 1) {
+    #pragma unroll
+    for (int j = 0; j < NV; j++)
+      if (act[j]) prefetch_l2(B + (int64_t)c * a.N + col0 + j * V);
+  } else if constexpr (SS_SR_PF_MODE == 2) {
+    prefetch_l2_bulk(B + (int64_t)c * a.N + tile_col0, tile_bytes);
+  }
+}
+
 // Returns false when a bounded wait expired (the caller then stops).
 template <typename T, typename TC, int V, int NV, bool KAHAN>
 __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
@@ -201,6 +226,12 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
   if (nst > 1) stage_issue<T, false>(a, st, L, 1, ci.cs + L.S, min(L.S, ci.ce - ci.cs - L.S), lane, G, mask, strm);
 
   // first row: lb = first row starting at or after cs
+  // bulk prefetch needs 16-byte aligned rows and slices
+  const int tile_col0 = blockIdx.y * a.col_tile;
+  const uint32_t tile_bytes = (uint32_t)(min(a.col_tile, a.N - tile_col0) * (int)sizeof(T));
+  const bool pf_on = SS_SR_PF_MODE == 1 ||
+                     (SS_SR_PF_MODE == 2 && ((uintptr_t)B & 15) == 0 && ((a.N * (int)sizeof(T)) & 15) == 0 &&
+                      ((tile_col0 * (int)sizeof(T)) & 15) == 0 && (tile_bytes & 15) == 0);
   const int lb = group_lower_bound(a.indptr, a.M, ci.cs, lane, G, mask);
   int win_base = lb;
   auto win_fill = [&](int base) {
@@ -273,6 +304,15 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
       // ---- label the tile's nonzeros with row | end-of-row bit; empty rows
       // starting where a row's first nonzero sits are zeroed by the whole
       // group (each lane owns one column slice)
+      if (SS_SR_PF_MODE != 0 && pf_on) {  // the first rows the walk will gather
+        if (SS_SR_PF_MODE == 1) {
+          for (int u = 0; u < SS_SR_PF_DIST && u < n; u++)
+            sr_prefetch_row<T, V, NV>(a, B, scol[u], col0, act, tile_col0, tile_bytes);
+        } else if (lane < SS_SR_PF_DIST && lane < n) {
+          for (int u = lane; u < SS_SR_PF_DIST && u < n; u += G)
+            sr_prefetch_row<T, V, NV>(a, B, scol[u], col0, act, tile_col0, tile_bytes);
+        }
+      }
       const int c0 = cur - win_base;
       const int rounds = (n + G - 1) / G;
       for (int k = 0; k < rounds; k++) {
@@ -307,6 +347,16 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
       __syncwarp(mask);
       // ---- walk: gather, multiply, store at row ends
       for (int q = 0; q < n; q += SR_U) {
+        if (SS_SR_PF_MODE != 0 && pf_on) {
+          if (SS_SR_PF_MODE == 1) {
+            #pragma unroll
+            for (int u = 0; u < SR_U; u++)
+              if (q + SS_SR_PF_DIST + u < n)
+                sr_prefetch_row<T, V, NV>(a, B, scol[q + SS_SR_PF_DIST + u], col0, act, tile_col0, tile_bytes);
+          } else if (lane < SR_U && q + SS_SR_PF_DIST + lane < n) {
+            sr_prefetch_row<T, V, NV>(a, B, scol[q + SS_SR_PF_DIST + lane], col0, act, tile_col0, tile_bytes);
+          }
+        }
         float bv[SR_U][NV][V];
         #pragma unroll
         for (int u = 0; u < SR_U; u++) {
