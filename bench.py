@@ -330,6 +330,47 @@ def extra_batched(dev, N=64, count=512):
     return res
 
 
+def _cusparse_ms(A, B, stream):
+    """cuSPARSE CSR SpMM through torch.sparse.mm on the same matrix (comparison line)."""
+    import torch
+    At = torch.sparse_csr_tensor(A.indptr.long(), A.indices.long(), A.values, (A.nrow, A.ncol))
+    return _event_ms(lambda: torch.sparse.mm(At, B), 10, stream)
+
+
+def extra_sweep(A_pl, dev):
+    """Every configuration's shape through the tuned strategy, with cuSPARSE
+    beside it: power-law 1e6 at N = 4, 16, 64, 128; banded 120k x 120k
+    (20 per row, half-width 500) at N = 64; Poisson(16) 4096 x 4096 at
+    N = 4, 16 (L2-resident and launch bound: no roofline meaning)."""
+    import torch
+    from segscan_gb300 import api, autotune, synth
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+    cases = [("powerlaw_1e6", A_pl, N) for N in (4, 16, 64, 128)]
+    cases.append(("banded_120k", synth.banded(120_000, 120_000, 20, 500, seed=1), 64))
+    P = synth.poisson(4096, 4096, 16.0, seed=0)
+    cases += [("poisson_4096", P, 4), ("poisson_4096", P, 16)]
+    for name, A, N in cases:
+        Ad = api.CsrMatrix.from_host(A, dev)
+        B = torch.from_numpy(synth.dense(A.ncol, N, seed=2)).to(dev)
+        strategy, k = autotune.best(Ad, N, B)
+        C = torch.empty((A.nrow, N), device=dev)
+        n = api.spmm_workspace_size(Ad, N, strategy, k)
+        ws = torch.empty(n + 256, dtype=torch.uint8, device=dev) if n else None
+        ms = _event_ms(lambda: api.spmm(Ad, B, strategy, knobs=k, out=C, workspace=ws), 20, stream)
+        nb = synth.spmm_bytes(A, N)
+        entry = {"nnz": A.nnz, "ms": ms, "GB/s": nb / ms / 1e6, "strategy": strategy, "knobs": k.as_dict()}
+        try:
+            cs = _cusparse_ms(Ad, B, stream)
+            entry.update({"cusparse_ms": cs, "speedup_vs_cusparse": cs / ms})
+        except Exception as exc:
+            entry["cusparse_error"] = f"{type(exc).__name__}: {exc}"
+        res[f"{name}_n{N}"] = entry
+        del Ad, B, C, ws
+        torch.cuda.empty_cache()
+    return res
+
+
 def extra_fwd_bwd(dev, N=128):
     """Differentiated SpMM layer: power-law 2e6 x 2e6 (Zipf 2.1 clipped to
     [1, 50000], seed 4), B 2e6 x 128, dC ~ N(0, 1).  Forward C = A B;
@@ -542,7 +583,8 @@ def run_ours(args):
     }
     if ws_ == 1 and args.extras:
         configs = {}
-        for key, fn in (("precision_powerlaw_n64", lambda: extra_precision(A, B, N, t * 1e3, dev)),
+        for key, fn in (("sweep_vs_cusparse", lambda: extra_sweep(A, dev)),
+                        ("precision_powerlaw_n64", lambda: extra_precision(A, B, N, t * 1e3, dev)),
                         ("batched_512", lambda: extra_batched(dev)),
                         ("fwd_bwd_powerlaw_2e6_n128", lambda: extra_fwd_bwd(dev))):
             try:
@@ -558,6 +600,11 @@ def run_ours(args):
         line["cpu_baseline"] = {"value": synth.spmm_bytes(sample, N) / sec / 1e9, "unit": UNIT, "cores": threads,
                                 "kind": "port", "sample": f"{desc}, {iters} passes, row-parallel restatement of "
                                                           "spmm_reference_host (check.cuh:139-158)"}
+        # the reference's check loop as written runs on one thread: a separate line
+        sample1, desc1, _ = cpu_sample(A, B, 2.0, 1)
+        sec1, iters1 = cpu_spmm_time(sample1, B, 1, 4.0)
+        line["cpu_baseline_single_thread"] = {"value": synth.spmm_bytes(sample1, N) / sec1 / 1e9, "unit": UNIT,
+                                              "cores": 1, "kind": "port", "sample": f"{desc1}, {iters1} passes"}
     print(json.dumps(line), flush=True)
 
 

@@ -73,11 +73,16 @@ static ss_status batch_layout(int count, const ss_csr *mats, int N, const ss_kno
   size_t o = 0;
   h.mats_off = o; o += a256(sizeof(BatchMat) * (size_t)count);
   h.item_mat_off = o; o += a256(4 * (size_t)items);
-  h.rows_off = o; o += a256(4 * (size_t)items);
+  // arrival counts per (item, column tile), then the work counters: one
+  // memset per step clears both
+  h.rows_off = o; o += 4 * (size_t)items * (size_t)(h.tiles > 0 ? h.tiles : 1);
+  h.counter_off = o; o = a256(o + 4 * (size_t)(h.tiles > 0 ? h.tiles : 1));
   h.heads_off = o; o += a256(4 * (size_t)items * N);
   h.tails_off = o; o += a256(4 * (size_t)items * N);
-  h.counter_off = o; o += a256(4 * (size_t)(h.tiles > 0 ? h.tiles : 1));
   h.dev_bytes = o;
+  // the walk stores head/tail partials as vectors of up to 32 bytes
+  if ((h.heads_off | h.tails_off | h.mats_off | h.item_mat_off | h.rows_off) & 255)
+    return fail(SS_ERR_INVALID_ARG, "internal: misaligned batch plan layout");
   return SS_OK;
 }
 
@@ -162,26 +167,14 @@ ss_status ss_spmm_batched(const void *host_plan, void *dev_plan, void *stream) {
   long long grid = (long long)per_sm * sm_count_batched();
   const long long need = ((long long)h.total_items + h.workers_per_block - 1) / h.workers_per_block;
   if (grid > need) grid = need;
-  e = cudaMemsetAsync((char *)dev_plan + h.counter_off, 0, 4 * (size_t)(h.tiles > 0 ? h.tiles : 1), s);
+  // arrival counts and work counters (adjacent in the plan)
+  e = cudaMemsetAsync((char *)dev_plan + h.rows_off, 0, h.heads_off - h.rows_off, s);
   if (e != cudaSuccess) return cuda_fail(e, "batched counter reset");
   int *err_ptr = walk_error_ptr();
   const char *plan = (const char *)dev_plan;
   void *args[] = {&plan, &h, &err_ptr};
   e = cudaLaunchKernel(fn, dim3((unsigned)grid, (unsigned)h.tiles, 1), dim3(h.block, 1, 1), args, h.smem, s);
-  if (e != cudaSuccess) return cuda_fail(e, "batched launch");
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)std::max(1, std::min((h.total_items + 7) / 8, 152 * 32)), 1, 1);
-  cfg.blockDim = dim3(256, 1, 1);
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  if (h.c_dtype == SS_F32) e = cudaLaunchKernelEx(&cfg, batched_fixup_kernel<float>, plan, h);
-  else if (h.c_dtype == SS_BF16) e = cudaLaunchKernelEx(&cfg, batched_fixup_kernel<__nv_bfloat16>, plan, h);
-  else e = cudaLaunchKernelEx(&cfg, batched_fixup_kernel<__half>, plan, h);
-  return e == cudaSuccess ? SS_OK : cuda_fail(e, "batched fix-up launch");
+  return e == cudaSuccess ? SS_OK : cuda_fail(e, "batched launch");
 }
 
 }  // extern "C"

@@ -8,9 +8,10 @@
 // wave; every group takes the next item from a device counter (atomicAdd,
 // no waiting on other groups) and walks it with the ebsr chunk walk
 // (eb_walk.cuh) against that matrix's arrays.  Straddling rows go to the
-// matrix's head/tail slots and one batched fix-up launch assembles them.
+// matrix's head/tail slots and the last of their chunks to finish
+// assembles them (carry_arrive), so one launch does the whole step.
 // Matrices without nonzeros get a zero-fill item.  The whole step (counter
-// reset, walk, fix-up) is stream-ordered and can be captured in a graph.
+// reset, walk) is stream-ordered and can be captured in a graph.
 #pragma once
 #include "eb_walk.cuh"
 
@@ -118,33 +119,14 @@ __global__ void __launch_bounds__(512, SS_SR_MIN_BLOCKS) batched_kernel(const ch
     a.chunk = mt.chunk;
     a.num_chunks = mt.num_chunks;
     a.use_tma = mt.use_tma;
-    a.carry_rows = rows_all + mt.item_begin;
+    a.carry_rows = nullptr;
+    a.carry_cnt = rows_all + (size_t)mt.item_begin * h.tiles;
     a.carry_vals = heads_all + (size_t)mt.item_begin * h.N;
     a.tail_vals = tails_all + (size_t)mt.item_begin * h.N;
     const bool done = a.chunk > h.kahan
                           ? sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm)
                           : sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
     if (!done) break;  // a bounded wait expired
-  }
-}
-
-template <typename TC>
-__global__ void __launch_bounds__(256) batched_fixup_kernel(const char *plan, BatchHeader h) {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  const BatchMat *mats = reinterpret_cast<const BatchMat *>(plan + h.mats_off);
-  const int32_t *item_mat = reinterpret_cast<const int32_t *>(plan + h.item_mat_off);
-  const int32_t *rows_all = reinterpret_cast<const int32_t *>(plan + h.rows_off);
-  const float *heads_all = reinterpret_cast<const float *>(plan + h.heads_off);
-  const float *tails_all = reinterpret_cast<const float *>(plan + h.tails_off);
-  const int lane = threadIdx.x & 31;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < h.total_items; i += warps) {
-    const BatchMat &mt = mats[item_mat[i]];
-    if (mt.nnz == 0 || mt.num_chunks <= 1) continue;
-    const int c = i - mt.item_begin;
-    fixup_chunk<TC>(rows_all + mt.item_begin, heads_all + (size_t)mt.item_begin * h.N,
-                    tails_all + (size_t)mt.item_begin * h.N, mt.num_chunks, h.N, mt.M, (TC *)mt.C, SS_SUM, 0,
-                    nullptr, 0, c, lane);
   }
 }
 

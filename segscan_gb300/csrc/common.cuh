@@ -247,15 +247,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
-// L2 prefetch of the line holding p (no register destination, no completion)
-__device__ __forceinline__ void prefetch_l2(const void *p) {
-  asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(p));
-}
-// L2 prefetch of [p, p + bytes) through the bulk-copy unit; p 16-byte
-// aligned, bytes a multiple of 16
-__device__ __forceinline__ void prefetch_l2_bulk(const void *p, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
   uint32_t ok;
   asm volatile(

@@ -14,14 +14,17 @@
 
 namespace ss {
 
-size_t eb_workspace_bytes(const EbGeom &g, int N) {
-  size_t rows = ((size_t)g.num_chunks * sizeof(int32_t) + 255) & ~(size_t)255;
-  return rows + 2 * (size_t)g.num_chunks * (size_t)N * sizeof(float);
+size_t carry_rows_bytes(int num_chunks, int tiles) {
+  return ((size_t)num_chunks * (size_t)std::max(1, tiles) * sizeof(int32_t) + 255) & ~(size_t)255;
 }
 
-CarryView carry_view(void *ws, int num_chunks, int N) {
+size_t eb_workspace_bytes(const EbGeom &g, int N) {
+  return carry_rows_bytes(g.num_chunks, g.cs.tiles) + 2 * (size_t)g.num_chunks * (size_t)N * sizeof(float);
+}
+
+CarryView carry_view(void *ws, int num_chunks, int N, int tiles) {
   CarryView cv;
-  size_t rows = ((size_t)num_chunks * sizeof(int32_t) + 255) & ~(size_t)255;
+  size_t rows = carry_rows_bytes(num_chunks, tiles);
   cv.rows = (int32_t *)ws;
   cv.vals = (float *)((char *)ws + rows);
   cv.tails = cv.vals + (size_t)num_chunks * (size_t)N;
@@ -43,10 +46,11 @@ EbArgs eb_base_args(const EbGeom &g, void *ws, int N) {
   a.use_tma = 0;
   a.err = nullptr;
   a.keep_frac = 1.0f;
-  CarryView cv = carry_view(ws, g.num_chunks, N);
+  CarryView cv = carry_view(ws, g.num_chunks, N, g.cs.tiles);
   a.carry_rows = cv.rows;
   a.carry_vals = cv.vals;
   a.tail_vals = cv.tails;
+  a.carry_cnt = cv.rows;
   return a;
 }
 
@@ -59,17 +63,32 @@ __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restr
   // launched as a programmatic dependent of the walk kernel: wait until the
   // walk's writes (head/tail slots, owner rows) are complete and visible
   asm volatile("griddepcontrol.wait;" ::: "memory");
+  // a warp scans 32 consecutive chunks at once (one coalesced read of their
+  // head rows), then assembles the runs that lead there one after another
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += warps)
-    fixup_chunk<TC>(rows, heads, tails, num_chunks, N, M, C, reduce, accumulate, index, nnz, c, lane);
+  for (int c0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; c0 < num_chunks; c0 += warps * 32) {
+    const int c = c0 + lane;
+    bool lead = false;
+    if (c > 0 && c < num_chunks) {
+      const int r = rows[c];
+      lead = r >= 0 && r < M && rows[c - 1] != r;
+    }
+    unsigned leaders = __ballot_sync(0xffffffffu, lead);
+    while (leaders) {
+      const int l = __ffs(leaders) - 1;
+      leaders &= leaders - 1;
+      fixup_chunk<TC>(rows, heads, tails, num_chunks, N, M, C, reduce, accumulate, index, nnz, c0 + l, lane);
+    }
+  }
 }
 
 ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *C, int c_dtype,
                        int reduce, int accumulate, const int32_t *index, int nnz, cudaStream_t s) {
   if (num_chunks <= 1 || N == 0 || M == 0) return SS_OK;  // chunk 0 never carries
   const int threads = 256;
-  const int blocks = std::max(1, std::min((num_chunks + 7) / 8, 152 * 32));
+  const int warps_needed = (num_chunks + 31) / 32;
+  const int blocks = std::max(1, std::min((warps_needed + 7) / 8, 152 * 8));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks, 1, 1);
   cfg.blockDim = dim3(threads, 1, 1);

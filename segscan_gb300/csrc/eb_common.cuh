@@ -42,6 +42,7 @@ struct EbArgs {
   int32_t *carry_rows;  // [num_chunks] head row of each chunk, -1 = none
   float *carry_vals;    // [num_chunks * N] head-row partials
   float *tail_vals;     // [num_chunks * N] partial of a last row that continues
+  int *carry_cnt;       // [num_chunks * column tiles] arrivals per straddling row (zeroed per launch)
 };
 
 struct ChunkInfo {
@@ -144,6 +145,71 @@ __device__ __forceinline__ void flush_row(const EbArgs &a, const ChunkInfo &ci, 
       for (int i = 0; i < V; i++) out[i] += prev[i];
     }
     store_vec<TC, V>(dst, out, pol);
+  }
+}
+
+// V floats from a carry slot written by other blocks in this launch: read
+// at L2 (ld.global.cg), never from a possibly stale L1 line.
+template <int V>
+__device__ __forceinline__ void load_slot(const float *p, float (&out)[V]) {
+  if constexpr (V == 1) {
+    out[0] = __ldcg(p);
+  } else if constexpr (V == 2) {
+    const float2 x = __ldcg(reinterpret_cast<const float2 *>(p));
+    out[0] = x.x; out[1] = x.y;
+  } else {
+    #pragma unroll
+    for (int i = 0; i < V; i += 4) {
+      const float4 x = __ldcg(reinterpret_cast<const float4 *>(p + i));
+      out[i] = x.x; out[i + 1] = x.y; out[i + 2] = x.z; out[i + 3] = x.w;
+    }
+  }
+}
+
+// In-kernel carry fix-up of the SpMM walks.  Row r straddles chunks o..l
+// (o holds its first nonzero and left r's partial in its tail slot; o+1..l
+// left theirs in their head slots).  Each of the l - o + 1 participants
+// calls this after storing its slot; the last to arrive (atomic count per
+// owner chunk and column tile) sums tail(o) + heads(o+1..l) in chunk order
+// with compensation, adds the old output in accumulate mode and stores the
+// row once - the same arithmetic, in the same order, as fixup_chunk, so the
+// result does not depend on which participant finishes last.  Nothing
+// waits: a participant that is not last returns at once.
+template <typename TC, int V, int NV>
+__device__ __forceinline__ void carry_arrive(const EbArgs &a, int r, int lane, int G, unsigned mask, int col0,
+                                          const bool (&act)[NV], uint64_t pol) {
+  const int o = __ldg(a.indptr + r) / a.chunk;
+  const int l = (__ldg(a.indptr + r + 1) - 1) / a.chunk;
+  int *cnt = a.carry_cnt + (size_t)o * gridDim.y + blockIdx.y;
+  __threadfence();  // this lane's slot stores are visible before the count moves
+  __syncwarp(mask);
+  int last = 0;
+  if (lane == 0) last = atomicAdd(cnt, 1) == l - o;
+  last = __shfl_sync(mask, last, 0, G);
+  if (!last) return;
+  __threadfence();  // every other participant's slot is visible now
+  TC *C = (TC *)a.C;
+  #pragma unroll
+  for (int j = 0; j < NV; j++) {
+    if (!act[j]) continue;
+    const int64_t col = col0 + j * V;
+    float acc[V], comp[V], x[V];
+    load_slot<V>(a.tail_vals + (int64_t)o * a.N + col, acc);
+    #pragma unroll
+    for (int i = 0; i < V; i++) comp[i] = 0.f;
+    for (int k = o + 1; k <= l; k++) {
+      load_slot<V>(a.carry_vals + (int64_t)k * a.N + col, x);
+      #pragma unroll
+      for (int i = 0; i < V; i++) kahan_add(acc[i], comp[i], x[i]);
+    }
+    TC *dst = C + (int64_t)r * a.N + col;
+    if (a.accumulate) {
+      float prev[V];
+      load_out<TC, V>(dst, prev);
+      #pragma unroll
+      for (int i = 0; i < V; i++) acc[i] += prev[i];
+    }
+    store_vec<TC, V>(dst, acc, pol);
   }
 }
 

@@ -161,7 +161,7 @@ ss_status launch_ebpr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
     fn = c.c_dtype == SS_F32 ? pr_ptr<__half, float, false>(g.cs.V) : pr_ptr<__half, __half, false>(g.cs.V);
   ss_status st = run_pr(fn, a, g, s, "ebpr launch");
   if (st != SS_OK) return st;
-  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.M, c.C, c.c_dtype, SS_SUM, c.accumulate,
+  return launch_fixup(carry_view(ws, g.num_chunks, c.N, g.cs.tiles), g.num_chunks, c.N, c.M, c.C, c.c_dtype, SS_SUM, c.accumulate,
                       nullptr, c.nnz, s);
 }
 
@@ -176,7 +176,7 @@ ss_status launch_seg_pr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_
   else fn = pr_ptr<__half, float, true>(g.cs.V);
   ss_status st = run_pr(fn, a, g, s, "segment_coo pr launch");
   if (st != SS_OK) return st;
-  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce, c.accumulate,
+  return launch_fixup(carry_view(ws, g.num_chunks, c.N, g.cs.tiles), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce, c.accumulate,
                       c.index, c.nnz, s);
 }
 

@@ -70,11 +70,13 @@ ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
   if (c.val_dtype == SS_F32) fn = sr_kernel_f32(g.cs.V, g.cs.NV, false);
   else if (c.val_dtype == SS_BF16) fn = sr_kernel_bf16(g.cs.V, g.cs.NV, false, c.c_dtype == SS_F32);
   else fn = sr_kernel_f16(g.cs.V, g.cs.NV, false, c.c_dtype == SS_F32);
-  ss_status st = run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, dtype_size(c.val_dtype)), s,
-                        "ebsr launch");
-  if (st != SS_OK) return st;
-  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.M, c.C, c.c_dtype, SS_SUM,
-                      c.accumulate, nullptr, c.nnz, s);
+  // straddling rows are assembled inside the walk (carry_arrive): only the
+  // arrival counts need zeroing, no fix-up launch follows
+  if (g.num_chunks > 0) {
+    cudaError_t e = cudaMemsetAsync(a.carry_cnt, 0, carry_rows_bytes(g.num_chunks, g.cs.tiles), s);
+    if (e != cudaSuccess) return cuda_fail(e, "ebsr carry counts");
+  }
+  return run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, dtype_size(c.val_dtype)), s, "ebsr launch");
 }
 
 ss_status launch_seg_sr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_t s) {
@@ -90,7 +92,7 @@ ss_status launch_seg_sr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_
   else fn = sr_kernel_f16(g.cs.V, g.cs.NV, true, true);
   ss_status st = run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, 0), s, "segment_coo sr launch");
   if (st != SS_OK) return st;
-  return launch_fixup(carry_view(ws, g.num_chunks, c.N), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce,
+  return launch_fixup(carry_view(ws, g.num_chunks, c.N, g.cs.tiles), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce,
                       c.accumulate, c.index, c.nnz, s);
 }
 

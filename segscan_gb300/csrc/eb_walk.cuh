@@ -37,16 +37,6 @@ namespace ss {
 #ifndef SS_SR_MIN_BLOCKS
 #define SS_SR_MIN_BLOCKS 2
 #endif
-// L2 prefetch of B rows SS_SR_PF_DIST nonzeros ahead of the gathers:
-// mode 1 = every lane prefetches its own slice (prefetch.global.L2),
-// mode 2 = one lane per row prefetches the group's whole slice of the row
-// (cp.async.bulk.prefetch.L2); 0 = off
-#ifndef SS_SR_PF_MODE
-#define SS_SR_PF_MODE 0
-#endif
-#ifndef SS_SR_PF_DIST
-#define SS_SR_PF_DIST 16
-#endif
 constexpr int SR_U = SS_SR_GATHER;            // B rows gathered ahead
 constexpr uint32_t SR_SPIN_LIMIT = 1u << 22;  // try_wait polls before giving up
 
@@ -195,21 +185,6 @@ __device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)
   }
 }
 
-// Prefetches into L2 the B row of staged nonzero column c (mode 1: this
-// lane's slice; mode 2: the group's slice, issued by one lane).
-template <typename T, int V, int NV>
-__device__ __forceinline__ void sr_prefetch_row(const EbArgs &a, const T *B, int c, int col0, const bool (&act)[NV],
-                                                int tile_col0, uint32_t tile_bytes) {
-  if ((unsigned)c >= (unsigned)a.K) return;
-  if constexpr (SS_SR_PF_MODE == 1) {
-    #pragma unroll
-    for (int j = 0; j < NV; j++)
-      if (act[j]) prefetch_l2(B + (int64_t)c * a.N + col0 + j * V);
-  } else if constexpr (SS_SR_PF_MODE == 2) {
-    prefetch_l2_bulk(B + (int64_t)c * a.N + tile_col0, tile_bytes);
-  }
-}
-
 // Returns false when a bounded wait expired (the caller then stops).
 template <typename T, typename TC, int V, int NV, bool KAHAN>
 __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
@@ -218,6 +193,10 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
   const T *__restrict__ B = (const T *)a.B;
   const int G = a.team_lanes;
   const bool ones = a.vals == nullptr;
+  // B rows gathered ahead: four, or two when a lane holds 8+ elements of a
+  // row (the gathered values then need as many registers)
+  constexpr int SR_FU = V * NV >= 8 ? 2 : 4;
+  constexpr int SR_UP = V * NV >= 8 ? 2 : SR_U;
   ChunkInfo ci;
   ci.cs = chunk * a.chunk;
   ci.ce = min(ci.cs + a.chunk, a.nnz);
@@ -226,12 +205,6 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
   if (nst > 1) stage_issue<T, false>(a, st, L, 1, ci.cs + L.S, min(L.S, ci.ce - ci.cs - L.S), lane, G, mask, strm);
 
   // first row: lb = first row starting at or after cs
-  // bulk prefetch needs 16-byte aligned rows and slices
-  const int tile_col0 = blockIdx.y * a.col_tile;
-  const uint32_t tile_bytes = (uint32_t)(min(a.col_tile, a.N - tile_col0) * (int)sizeof(T));
-  const bool pf_on = SS_SR_PF_MODE == 1 ||
-                     (SS_SR_PF_MODE == 2 && ((uintptr_t)B & 15) == 0 && ((a.N * (int)sizeof(T)) & 15) == 0 &&
-                      ((tile_col0 * (int)sizeof(T)) & 15) == 0 && (tile_bytes & 15) == 0);
   const int lb = group_lower_bound(a.indptr, a.M, ci.cs, lane, G, mask);
   int win_base = lb;
   auto win_fill = [&](int base) {
@@ -260,7 +233,6 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
   ci.r_first = cur;
   ci.r_last = cur;
   ci.prev_row = -1;
-  if (blockIdx.y == 0 && lane == 0) a.carry_rows[chunk] = ci.has_head ? cur : -1;
   const int head = ci.has_head ? cur : -1;
 
   bool open = false;
@@ -304,21 +276,14 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
       // ---- label the tile's nonzeros with row | end-of-row bit; empty rows
       // starting where a row's first nonzero sits are zeroed by the whole
       // group (each lane owns one column slice)
-      if (SS_SR_PF_MODE != 0 && pf_on) {  // the first rows the walk will gather
-        if (SS_SR_PF_MODE == 1) {
-          for (int u = 0; u < SS_SR_PF_DIST && u < n; u++)
-            sr_prefetch_row<T, V, NV>(a, B, scol[u], col0, act, tile_col0, tile_bytes);
-        } else if (lane < SS_SR_PF_DIST && lane < n) {
-          for (int u = lane; u < SS_SR_PF_DIST && u < n; u += G)
-            sr_prefetch_row<T, V, NV>(a, B, scol[u], col0, act, tile_col0, tile_bytes);
-        }
-      }
       const int c0 = cur - win_base;
       const int rounds = (n + G - 1) / G;
+      bool bad = false;  // a column outside [0, K) in this tile
       for (int k = 0; k < rounds; k++) {
         const int e = lane + k * G;
         int zlo = 0, zhi = -1;
         if (e < n) {
+          bad |= (unsigned)scol[e] >= (unsigned)a.K;
           const int p = sb + e;
           int lo = c0 + 1, hi = L.W - 1;
           while (lo < hi) {
@@ -344,22 +309,60 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
           todo &= todo - 1;
         }
       }
-      __syncwarp(mask);
-      // ---- walk: gather, multiply, store at row ends
-      for (int q = 0; q < n; q += SR_U) {
-        if (SS_SR_PF_MODE != 0 && pf_on) {
-          if (SS_SR_PF_MODE == 1) {
+      __syncwarp(mask);  // labels written by every lane are visible to the group
+      // a full tile of valid columns takes the lean loop: four staged
+      // columns, labels and values per shared-memory read, no bounds checks
+      const bool full = n == L.S && !__any_sync(mask, bad);
+      auto consume = [&](int info, float v, const float (&b)[NV][V]) {
+        add_row<V, NV, KAHAN>(acc, comp, v, b);
+        cur = info & 0x7fffffff;
+        open = true;
+        if (info < 0) {
+          flush_done(cur);
+          open = false;
+        }
+      };
+      if (full) {
+        const int4 *col4 = reinterpret_cast<const int4 *>(scol);
+        const int4 *info4 = reinterpret_cast<const int4 *>(sinfo);
+        for (int q = 0; q < n; q += 4) {
+          const int4 cc = col4[q >> 2];
+          const int4 in4 = info4[q >> 2];
+          const int cs4[4] = {cc.x, cc.y, cc.z, cc.w};
+          const int is4[4] = {in4.x, in4.y, in4.z, in4.w};
+          float v4[4];
+          if (ones) {
+            v4[0] = v4[1] = v4[2] = v4[3] = 1.f;
+          } else if constexpr (sizeof(T) == 4) {
+            const float4 x = *reinterpret_cast<const float4 *>(sval + q);
+            v4[0] = x.x; v4[1] = x.y; v4[2] = x.z; v4[3] = x.w;
+          } else {
+            const uint2 x = *reinterpret_cast<const uint2 *>(sval + q);
+            unpack2(x.x, v4[0], v4[1], (T *)nullptr);
+            unpack2(x.y, v4[2], v4[3], (T *)nullptr);
+          }
+          #pragma unroll
+          for (int h = 0; h < 4; h += SR_FU) {
+            float bv[SR_FU][NV][V];
             #pragma unroll
-            for (int u = 0; u < SR_U; u++)
-              if (q + SS_SR_PF_DIST + u < n)
-                sr_prefetch_row<T, V, NV>(a, B, scol[q + SS_SR_PF_DIST + u], col0, act, tile_col0, tile_bytes);
-          } else if (lane < SR_U && q + SS_SR_PF_DIST + lane < n) {
-            sr_prefetch_row<T, V, NV>(a, B, scol[q + SS_SR_PF_DIST + lane], col0, act, tile_col0, tile_bytes);
+            for (int u = 0; u < SR_FU; u++)
+              #pragma unroll
+              for (int j = 0; j < NV; j++) {
+                if (act[j]) {
+                  load_vec<T, V>(B + (int64_t)cs4[h + u] * a.N + col0 + j * V, bv[u][j], keep);
+                } else {
+                  #pragma unroll
+                  for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+                }
+              }
+            #pragma unroll
+            for (int u = 0; u < SR_FU; u++) consume(is4[h + u], v4[h + u], bv[u]);
           }
         }
-        float bv[SR_U][NV][V];
+      } else for (int q = 0; q < n; q += SR_UP) {  // ---- partial tile: gather, multiply, store at row ends
+        float bv[SR_UP][NV][V];
         #pragma unroll
-        for (int u = 0; u < SR_U; u++) {
+        for (int u = 0; u < SR_UP; u++) {
           const int c = q + u < n ? scol[q + u] : -1;
           const bool live = (unsigned)c < (unsigned)a.K;
           #pragma unroll
@@ -373,17 +376,9 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
           }
         }
         #pragma unroll
-        for (int u = 0; u < SR_U; u++) {
+        for (int u = 0; u < SR_UP; u++) {
           if (q + u >= n) break;
-          const int info = sinfo[q + u];
-          const float v = ones ? 1.f : Elem<T>::to_f(sval[q + u]);
-          add_row<V, NV, KAHAN>(acc, comp, v, bv[u]);
-          cur = info & 0x7fffffff;
-          open = true;
-          if (info < 0) {
-            flush_done(cur);
-            open = false;
-          }
+          consume(sinfo[q + u], ones ? 1.f : Elem<T>::to_f(sval[q + u]), bv[u]);
         }
       }
     } else {
@@ -437,18 +432,18 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
       stage_issue<T, false>(a, st, L, b, sb + 2 * L.S, min(L.S, ci.ce - sb - 2 * L.S), lane, G, mask, strm);
   }
   // the last row continues past the chunk: head slot or tail slot
+  const bool tail = open && cur != head;
   if (open) {
-    if (cur == head) {
-      #pragma unroll
-      for (int j = 0; j < NV; j++)
-        if (act[j]) store_vec<float, V>(a.carry_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], strm);
-    } else {
-      #pragma unroll
-      for (int j = 0; j < NV; j++)
-        if (act[j]) store_vec<float, V>(a.tail_vals + (int64_t)chunk * a.N + col0 + j * V, acc[j], strm);
-    }
+    float *slot = (cur == head ? a.carry_vals : a.tail_vals) + (int64_t)chunk * a.N + col0;
+    #pragma unroll
+    for (int j = 0; j < NV; j++)
+      if (act[j]) store_vec<float, V>(slot + j * V, acc[j], strm);
   }
   if (!a.accumulate && ci.ce >= a.nnz) zero_rows<TC, V, NV>(a, cur + 1, a.M - 1, col0, act, strm);
+  // the head row's partial was stored (at its end, or just above): count
+  // this chunk in for the head row and, when it has one, the tail row
+  if (head >= 0) carry_arrive<TC, V, NV>(a, head, lane, G, mask, col0, act, strm);
+  if (tail) carry_arrive<TC, V, NV>(a, cur, lane, G, mask, col0, act, strm);
   return true;
 }
 

@@ -91,11 +91,14 @@ ss_status launch_seg_pr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_
 
 // Carry fix-up shared by the element-balanced kernels (eb_common.cu).
 struct CarryView {
-  int32_t *rows;   // [num_chunks], -1 = no head row
+  int32_t *rows;   // [num_chunks], -1 = no head row (fix-up kernel path);
+                   // the same region is [num_chunks * tiles] arrival counts
+                   // for the walks that assemble straddling rows in-kernel
   float *vals;     // [num_chunks * N] head-row partials
   float *tails;    // [num_chunks * N] partials of rows continuing past a chunk
 };
-CarryView carry_view(void *ws, int num_chunks, int N);
+CarryView carry_view(void *ws, int num_chunks, int N, int tiles);
+size_t carry_rows_bytes(int num_chunks, int tiles);
 ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *C, int c_dtype,
                        int reduce, int accumulate, const int32_t *index, int nnz, cudaStream_t s);
 

@@ -60,6 +60,30 @@ def test_workspace_size_queries(lib):
     assert n.value > 0
 
 
+@pytest.mark.parametrize("N", [1, 3, 16, 33, 64, 100, 128, 256])
+def test_batch_plan_layout_sizes(lib, N):
+    """ss_batch_plan_size lays the plan out on the host (the layout checks
+    its own vector alignment) for item counts and column tilings of every
+    residue; the device buffer grows with the items."""
+    vec = 4 if N % 4 == 0 else 2 if N % 2 == 0 else 1  # one vector per lane, as batch_knobs picks
+    gf = min(5, max(0, (N // vec).bit_length() - 1))
+    sizes = []
+    for count in (1, 2, 3, 5, 7, 13):
+        mats = (SsCsr * count)(*[SsCsr(50 + 7 * i, 40 + 3 * i, 97 * (i + 1) + i * i, 256, 512, 1024, 0)
+                                  for i in range(count)])
+        knobs = (SsKnobs * count)()
+        for i in range(count):
+            assert lib.ss_default_knobs(2, N, ctypes.byref(knobs[i])) == 0
+            knobs[i].group_factor, knobs[i].coarsen_factor = gf, vec
+            knobs[i].thread_nz, knobs[i].block_denom = 1 + i % 5, 1
+        hb, db = ctypes.c_size_t(), ctypes.c_size_t()
+        assert lib.ss_batch_plan_size(count, mats, N, knobs, ctypes.byref(hb), ctypes.byref(db)) == 0, \
+            lib.ss_last_error()
+        assert db.value % 256 == 0 and hb.value > 0
+        sizes.append(db.value)
+    assert sizes == sorted(sizes)
+
+
 def test_bad_arguments_rejected_without_launch(lib):
     A = fake_csr()
     n = ctypes.c_size_t()
