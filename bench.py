@@ -294,17 +294,28 @@ def extra_batched(dev, N=64, count=512):
     res = {"matrices": count, "rows": int(sum(A.nrow for A in mats_h)), "nnz": int(sum(A.nnz for A in mats_h))}
     mats32 = [api.CsrMatrix.from_host(A, dev) for A in mats_h]
     B32 = [torch.from_numpy(b).to(dev) for b in Bh]
-    knobs32 = autotune.batch_knobs(mats32, N)
     outs = [torch.empty((A.nrow, N), device=dev) for A in mats_h]
-    wss = []
-    for A, k in zip(mats32, knobs32):
-        n = api.spmm_workspace_size(A, N, "ebsr", k)
-        wss.append(torch.empty(n + 256, dtype=torch.uint8, device=dev) if n else None)
-    plain = lambda: batched.plain_per_matrix(mats32, B32, outs, [("ebsr", k) for k in knobs32], wss)
-    plain_ms = _event_ms(plain, 3, stream, warm=1)
+    # the comparison: one ordinary launch per matrix, at the chunk size
+    # (128, 256 or 512 nonzeros) that makes those launches fastest; a small
+    # matrix is one short chain of dependent loads per chunk, so smaller
+    # chunks finish sooner
+    best = None
+    for target in (128, 256, 512):
+        knobs32 = autotune.batch_knobs(mats32, N, target)
+        wss = []
+        for A, k in zip(mats32, knobs32):
+            n = api.spmm_workspace_size(A, N, "ebsr", k)
+            wss.append(torch.empty(n + 256, dtype=torch.uint8, device=dev) if n else None)
+        plain = (lambda kk, ww: lambda: batched.plain_per_matrix(mats32, B32, outs, [("ebsr", k) for k in kk], ww))(
+            knobs32, wss)
+        ms = _event_ms(plain, 3, stream, warm=1)
+        if best is None or ms < best[0]:
+            best = (ms, target, plain)
+    plain_ms, plain_target, plain = best
     res["plain_fp32_per_matrix_ms"] = plain_ms
+    res["plain_chunk_target"] = plain_target
     # the same per-matrix launches replayed from one CUDA graph (no host
-    # overhead left: what remains is one walk + one fix-up launch per matrix)
+    # overhead left: what remains is one memset and one walk per matrix)
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):
         plain()

@@ -177,6 +177,15 @@ ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_byt
   g.workers_per_block = k.thread_per_block / G;
   g.block = k.thread_per_block;
   g.chunk = k.thread_nz * G;
+  // A group pays a chain of dependent loads to set up each chunk (first
+  // row search, first staged tile, row window), so chunks much smaller than
+  // the balanced share (nnz over the groups of one full wave on the 152 SMs
+  // at the walk's 1024 resident threads per SM) are merged up to that share:
+  // small thread_nz tuples then run as fast as tuned ones.
+  const long long wave_groups = 152LL * 1024 / G;
+  long long share = nnz > 0 ? ceil_div((long long)nnz, wave_groups) : 0;
+  share = ceil_div(share, 8LL * G) * 8LL * G;  // whole staged tiles keep the bulk copies aligned
+  if (share > g.chunk && share <= (1LL << 30)) g.chunk = (int)share;
   g.num_chunks = nnz > 0 ? ceil_div(nnz, g.chunk) : 0;
   // staged tile: 64 nonzeros, smaller when the block's groups would need
   // more than 48 KB of shared memory (a multiple of 8 keeps bulk copies
@@ -222,8 +231,15 @@ static ss_status geom_pr(long long worker_units, int nnz, int N, int dtype, cons
   if (steps < 1) steps = 1;
   g.chunk = (int)(steps * tile);
   g.num_chunks = nnz > 0 ? ceil_div(nnz, g.chunk) : 0;
-  g.stage = 0;
-  g.smem = 0;
+  // per tile-lane set, a shared-memory window of the chunk's row starts
+  // (chunk + 2 entries covers every chunk without empty rows), so the row of
+  // each nonzero is searched on chip; at most 48 KB per block
+  const long long sets = g.block / tile > 0 ? g.block / tile : 1;
+  long long w = (long long)g.chunk + 2;
+  const long long w_cap = (48LL * 1024 / 4) / sets;
+  if (w > w_cap) w = w_cap;
+  g.stage = w >= 4 ? (int)w : 0;
+  g.smem = (size_t)sets * (size_t)g.stage * 4;
   finish_eb(workers, g);
   return SS_OK;
 }

@@ -19,8 +19,21 @@
 
 namespace ss {
 
+// Row of nonzero p from the staged row starts win[i] = indptr[r_first + i],
+// i < nwin: the same upper_bound - 1 as row_search over [r_first + 1,
+// r_last + 1), read from shared memory.
+__device__ __forceinline__ int win_row(const int32_t *win, int nwin, int r_first, int p) {
+  int lo = 1, hi = nwin - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (win[mid] <= p) lo = mid + 1; else hi = mid;
+  }
+  return r_first + hi - 1;
+}
+
 template <typename T, typename TC, int V, bool SEG>
 __global__ void __launch_bounds__(1024) eb_pr_kernel(EbArgs a) {
+  extern __shared__ int32_t pr_win[];  // [tile-lane sets of the block][a.stage] (SpMM)
   const T *__restrict__ B = (const T *)a.B;
   const T *__restrict__ vals = (const T *)a.vals;
   const int tile = a.team_lanes;
@@ -37,9 +50,21 @@ __global__ void __launch_bounds__(1024) eb_pr_kernel(EbArgs a) {
   const float ident = is_max ? -INFINITY : 0.f;
   const int stride = gridDim.x * a.workers_per_block;
 
+  int32_t *win = pr_win + (size_t)(tid >> a.log2_team_lanes) * a.stage;
   for (int chunk = blockIdx.x * a.workers_per_block + wib; chunk < a.num_chunks; chunk += stride) {
     const ChunkInfo ci = chunk_info<SEG>(a, chunk);
     if (blockIdx.y == 0 && cg == 0 && lane == 0) a.carry_rows[chunk] = ci.has_head ? ci.r_first : -1;
+    // stage the chunk's row starts when they fit the window
+    int nwin = 0;
+    if (!SEG && a.stage > 0) {
+      const int need = ci.r_last - ci.r_first + 2;
+      __syncwarp(mask);  // the previous chunk's searches are done
+      if (need <= a.stage) {
+        nwin = need;
+        for (int i = lane; i < need; i += tile) win[i] = __ldg(a.indptr + ci.r_first + i);
+      }
+      __syncwarp(mask);
+    }
 
     // running segment carried across steps; without a head row it starts as
     // the row before the chunk, so the first step zeroes the gap after it
@@ -59,7 +84,7 @@ __global__ void __launch_bounds__(1024) eb_pr_kernel(EbArgs a) {
       #pragma unroll
       for (int i = 0; i < V; i++) x[0][i] = ident;
       if (live) {
-        row = chunk_row<SEG>(a, ci, p);
+        row = nwin ? win_row(win, nwin, ci.r_first, p) : chunk_row<SEG>(a, ci, p);
         int c;
         float v;
         if (SEG) {
@@ -141,7 +166,7 @@ static ss_status run_pr(void *fn, EbArgs &a, const EbGeom &g, cudaStream_t s, co
   if (!fn) return fail(SS_ERR_UNSUPPORTED_KNOBS, "no %s kernel for V=%d", what, g.cs.V);
   dim3 grid(g.grid_x, g.cs.tiles, 1), block(g.block, 1, 1);
   void *args[] = {&a};
-  cudaError_t err = cudaLaunchKernel(fn, grid, block, args, 0, s);
+  cudaError_t err = cudaLaunchKernel(fn, grid, block, args, g.smem, s);
   if (err != cudaSuccess) return cuda_fail(err, what);
   return SS_OK;
 }

@@ -162,23 +162,30 @@ __device__ __forceinline__ void rbpr_slot(const RbArgs &a, int s, int e, int slo
   const int S = a.slots;
   Acc<V, NV> comp;
   comp.zero();
-  for (int p0 = s + slot; p0 < e; p0 += 2 * S) {
-    int c[2];
-    float v[2];
-    float b[2][NV][V];
+  // four nonzeros per slot per step: their indices and values are loaded
+  // together, then their four B rows, so a long row costs two dependent
+  // round trips per four of its nonzeros on each slot
+  constexpr int U = 4;
+  for (int p0 = s + slot; p0 < e; p0 += U * S) {
+    int c[U];
+    float v[U];
+    float b[U][NV][V];
     #pragma unroll
-    for (int u = 0; u < 2; u++) {
+    for (int u = 0; u < U; u++) {
       const int p = p0 + u * S;
-      c[u] = 0;
+      c[u] = -1;
       v[u] = 0.f;
       if (p < e) {
         c[u] = ld_idx(a.indices + p, strm);
         v[u] = load_val<T>(vals, p, strm);
-        if ((unsigned)c[u] >= (unsigned)a.K) { c[u] = 0; v[u] = 0.f; }
       }
+    }
+    #pragma unroll
+    for (int u = 0; u < U; u++) {
+      if ((unsigned)c[u] >= (unsigned)a.K) { c[u] = -1; v[u] = 0.f; }  // past the row, or a bad column
       #pragma unroll
       for (int j = 0; j < NV; j++) {
-        if (p < e && act[j]) {
+        if (c[u] >= 0 && act[j]) {
           load_vec<T, V>(B + (int64_t)c[u] * a.N + col0 + j * V, b[u][j], keep);
         } else {
           #pragma unroll
@@ -187,7 +194,7 @@ __device__ __forceinline__ void rbpr_slot(const RbArgs &a, int s, int e, int slo
       }
     }
     #pragma unroll
-    for (int u = 0; u < 2; u++)
+    for (int u = 0; u < U; u++)
       #pragma unroll
       for (int j = 0; j < NV; j++)
         #pragma unroll

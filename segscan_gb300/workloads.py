@@ -7,7 +7,8 @@ synthetic matrices the benchmark configurations name.
 
 Cases: spmm-<strategy>-n<N> (strategy ebpr|rbpr|ebsr|rbsr, power-law
 1e6 x 1e6), spmm-ebsr-banded-n64, spmm-ebsr-bf16-n64, segment-<sr|pr>-<sum|max|mean>-n<N>
-(segments = the power-law matrix's rows), transpose, sddmm-n64, batched-bf16-n64.
+(segments = the power-law matrix's rows), transpose, sddmm-n64, batched-bf16-n64,
+batched-plain-n64 (the same 512 matrices, one launch each).
 --scale shrinks the matrices (rows / scale) for small profiling runs.
 """
 from __future__ import annotations
@@ -93,6 +94,21 @@ def run(case: str, iters: int, scale: int, knobs: dict | None = None) -> dict:
         Bd = torch.rand((A.ncol, N), device=dev)
         ms = _time(lambda: api.sddmm(Ad, dC, Bd), iters)
         nb = A.nnz * 12 + (A.nrow + 1) * 4 + A.nrow * N * 4 + A.distinct_columns() * N * 4
+    elif parts[0] == "batched" and parts[1] == "plain":
+        # the comparison for the batched launch: one ordinary launch per matrix
+        from . import batched
+        N = int(parts[-1][1:])
+        mats_h = synth.batch(max(8, 512 // scale), 100, 50_000, 2.3, 2000, seed=3)
+        mats = [api.CsrMatrix.from_host(A, dev) for A in mats_h]
+        Bs = [torch.rand((A.ncol, N), device=dev) for A in mats_h]
+        outs = [torch.empty((A.nrow, N), device=dev) for A in mats_h]
+        kn = autotune.batch_knobs(mats, N)
+        wss = []
+        for A, k in zip(mats, kn):
+            n = api.spmm_workspace_size(A, N, "ebsr", k)
+            wss.append(torch.empty(n + 256, dtype=torch.uint8, device=dev) if n else None)
+        ms = _time(lambda: batched.plain_per_matrix(mats, Bs, outs, [("ebsr", k) for k in kn], wss), iters)
+        nb = sum(synth.spmm_bytes(A, N) for A in mats_h)
     elif parts[0] == "batched":
         from . import batched
         N = int(parts[-1][1:])

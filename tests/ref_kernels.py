@@ -1,0 +1,89 @@
+"""Launches the reference's own SpMM kernels (test-cg/include/spmm/
+spmm_cg.cuh, compiled for sm_103a into oracle/_ref/ref_kernels.cubin by
+`make -C oracle ref`) through the CUDA driver API, with the launch geometry
+of the reference's launchers (spmm_cg.cuh:176-197, 333-353, 553-566,
+664-677) at its README-best static knobs for N = 64.  Test and measurement
+infrastructure only: the comparison line for this library's kernels."""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import torch
+
+CUBIN = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_kernels.cubin"
+
+
+def ceil_div(a, b):
+    return (a + b - 1) // b
+
+
+class RefKernels:
+    """The four reference kernels for N = 64 (float4 accesses)."""
+
+    N = 64
+
+    def __init__(self):
+        torch.cuda.init()
+        torch.empty(1, device="cuda")  # the primary context is current on this thread
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        self.mod = ctypes.c_void_p()
+        self._check(self.cu.cuModuleLoad(ctypes.byref(self.mod), str(CUBIN).encode()), "cuModuleLoad")
+        self.fn = {}
+        for name in ("ebpr", "rbpr", "ebsr", "rbsr"):
+            f = ctypes.c_void_p()
+            self._check(self.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, f"ref_{name}_n64".encode()),
+                        f"cuModuleGetFunction ref_{name}_n64")
+            self.fn[name] = f
+
+    @staticmethod
+    def available() -> bool:
+        return CUBIN.exists()
+
+    @staticmethod
+    def _check(rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} failed with CUresult {rc}")
+
+    def geometry(self, strategy: str, M: int, N: int):
+        """(grid, block, smem) the reference's launcher computes."""
+        assert N == self.N
+        if strategy == "ebpr":  # (5,256,5,1,16): group 32, tile 32
+            tile, tpb, factor = 32, 256, 1 / 16
+            cf = 4
+            ndim_tb = ceil_div(N, tile)
+            ndim_warp = min(N, tile) // cf
+            nnz_warp_per_tb = ceil_div(tpb // tile, ndim_warp)
+            return (ceil_div(int(M * factor), nnz_warp_per_tb), ndim_tb, 1), (ndim_warp * tile, nnz_warp_per_tb, 1), 0
+        if strategy == "rbpr":  # (3,256,3,1,2): group 8, tile 8
+            tile, tpb, factor = 8, 256, 1 / 2
+            cf = 4
+            ndim_tb = ceil_div(N, tile)
+            ndim_warp = min(N, tile) // cf
+            m_warp_per_tb = ceil_div(tpb // tile, ndim_warp)
+            return (ceil_div(int(M * factor), m_warp_per_tb), ndim_tb, 1), (ndim_warp * tile, m_warp_per_tb, 1), 0
+        if strategy == "ebsr":  # (4,256,4,1,1,16): group 16, CoarsenFactor 4, ThreadNz 1
+            group, tpb, factor = 16, 256, 1 / 16
+            coarsen = min(ceil_div(N, group), 4)
+            return (int(M * factor), ceil_div(N, group * coarsen), 1), (256, 1, 1), 12 * tpb
+        if strategy == "rbsr":  # coarsen 4, tile 2^5, 256 threads
+            tile, tpb, cf = 32, 256, 4
+            ndim_tb = ceil_div(N, tile)
+            nthr = min(N, tile) // cf
+            mthr = ceil_div(tpb, nthr)
+            return (ceil_div(M, mthr), ndim_tb, 1), (mthr, nthr, 1), 0
+        raise ValueError(strategy)
+
+    def launch(self, strategy: str, M: int, K: int, nnz: int, indptr, indices, data, B, C, stream=None):
+        """One launch (C must be zeroed first for all but rbsr, as the reference requires)."""
+        N = int(B.shape[1])
+        grid, block, smem = self.geometry(strategy, M, N)
+        ints = [ctypes.c_int(M), ctypes.c_int(N), ctypes.c_int(K)]
+        if strategy in ("ebpr", "ebsr"):
+            ints.append(ctypes.c_int(nnz))
+        ptrs = [ctypes.c_void_p(t.data_ptr()) for t in (indptr, indices, data, B, C)]
+        vals = ints + ptrs
+        params = (ctypes.c_void_p * len(vals))(*[ctypes.cast(ctypes.pointer(v), ctypes.c_void_p) for v in vals])
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        self._check(self.cu.cuLaunchKernel(self.fn[strategy], grid[0], grid[1], grid[2], block[0], block[1], block[2],
+                                           smem, ctypes.c_void_p(s), params, None), f"launch {strategy}")

@@ -47,7 +47,9 @@ def test_noalloc_rejects_oversize_scratch(lib):
     """A call whose scratch would exceed the fixed array is refused before any
     device work (the pointers here are never dereferenced)."""
     big = SsCsr(4_000_000, 4_000_000, 400_000_000, 256, 512, 1024, 0)
-    knobs = SsKnobs(4, 0, 256, 1, 1, 4, 1, 0)  # 16-nonzero chunks: 25 M chunks of carries
-    st = lib.ss_spmm_ebsr_noalloc(ctypes.byref(big), 64, 4096, 8192, 0, 0, ctypes.byref(knobs), None)
+    knobs = SsKnobs(4, 0, 256, 1, 1, 4, 1, 0)
+    # ~9.7 K chunks (one wave's share each) of 1024-wide head and tail
+    # partials: ~80 MB of carries
+    st = lib.ss_spmm_ebsr_noalloc(ctypes.byref(big), 1024, 4096, 8192, 0, 0, ctypes.byref(knobs), None)
     assert st == Status.CAPACITY
     assert b"fixed" in lib.ss_last_error()
