@@ -230,12 +230,25 @@ static ss_status geom_pr(long long worker_units, int nnz, int N, int dtype, cons
   long long steps = workers > 0 ? (steps_total + workers - 1) / workers : 1;
   if (steps < 1) steps = 1;
   g.chunk = (int)(steps * tile);
+  // chunks below the share of one full wave (1024 resident threads on each
+  // of the 152 SMs, shared by the column tiles) are merged up to it: each
+  // chunk costs a chain of dependent loads to set up (cf. geom_sr)
+  {
+    long long blocks_per_sm = 1024 / g.block;
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    long long wave = 152LL * blocks_per_sm * g.workers_per_block / (g.cs.tiles > 0 ? g.cs.tiles : 1);
+    if (wave < 1) wave = 1;
+    long long share = nnz > 0 ? ceil_div((long long)nnz, wave) : 0;
+    share = ceil_div(share, (long long)tile) * tile;
+    if (share > g.chunk && share <= (1LL << 30)) g.chunk = (int)share;
+  }
   g.num_chunks = nnz > 0 ? ceil_div(nnz, g.chunk) : 0;
-  // per tile-lane set, a shared-memory window of the chunk's row starts
-  // (chunk + 2 entries covers every chunk without empty rows), so the row of
-  // each nonzero is searched on chip; at most 48 KB per block
+  // per tile-lane set, a sliding shared-memory window of row starts, so the
+  // row of each nonzero is searched on chip: up to chunk + 2 entries (a chunk
+  // without empty rows fits), at most 256 + tile and 48 KB per block
   const long long sets = g.block / tile > 0 ? g.block / tile : 1;
   long long w = (long long)g.chunk + 2;
+  if (w > 256 + tile) w = 256 + tile;
   const long long w_cap = (48LL * 1024 / 4) / sets;
   if (w > w_cap) w = w_cap;
   g.stage = w >= 4 ? (int)w : 0;

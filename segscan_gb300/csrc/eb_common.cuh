@@ -213,6 +213,44 @@ __device__ __forceinline__ void carry_arrive(const EbArgs &a, int r, int lane, i
   }
 }
 
+// First r in [0, M] with indptr[r] >= key, found by all G lanes of the
+// group: each round every lane probes one of G split points of [lo, hi].
+__device__ __forceinline__ int group_lower_bound(const int32_t *indptr, int M, int key, int lane, int G,
+                                                 unsigned mask) {
+  int lo = 0, hi = M;  // answer in [lo, hi]
+  const unsigned lanes_bits = G >= 32 ? 0xffffffffu : ((1u << G) - 1u);
+  const unsigned shift = (threadIdx.x & 31u) & ~(unsigned)(G - 1);
+  while (lo < hi) {
+    const long long span = (long long)(hi - lo);
+    const int probe = lo + (int)((span * (lane + 1)) / (G + 1));
+    const bool ge = __ldg(indptr + probe) >= key;
+    const unsigned hits = (__ballot_sync(mask, ge) >> shift) & lanes_bits;
+    const int first = hits ? __ffs(hits) - 1 : G;  // first lane whose probe is >= key
+    const int nhi = first < G ? __shfl_sync(mask, probe, first, G) : hi;
+    const int nlo = first > 0 ? __shfl_sync(mask, probe, first - 1, G) + 1 : lo;
+    lo = nlo;
+    hi = nhi;
+  }
+  return lo;
+}
+
+// chunk_info for the SpMM path with the G lanes of a worker searching
+// together (group_lower_bound); the same rows as chunk_info<false>:
+// row_search(indptr, 1, M, e) is the first r >= 1 with indptr[r] > e, less
+// one, capped at M - 1, i.e. min(lower_bound(e + 1), M) - 1.
+__device__ __forceinline__ ChunkInfo chunk_info_group(const EbArgs &a, int chunk, int lane, int G, unsigned mask) {
+  ChunkInfo ci;
+  ci.cs = chunk * a.chunk;
+  ci.ce = min(ci.cs + a.chunk, a.nnz);
+  ci.r_first = min(group_lower_bound(a.indptr, a.M, ci.cs + 1, lane, G, mask), a.M) - 1;
+  ci.r_last = min(group_lower_bound(a.indptr, a.M, ci.ce, lane, G, mask), a.M) - 1;
+  ci.has_head = ci.cs > 0 && __ldg(a.indptr + ci.r_first) < ci.cs;
+  if (ci.cs == 0) ci.prev_row = -1;
+  else if (ci.has_head) ci.prev_row = ci.r_first;
+  else ci.prev_row = min(group_lower_bound(a.indptr, a.M, ci.cs, lane, G, mask), a.M) - 1;
+  return ci;
+}
+
 __device__ __forceinline__ int lower_bound_idx(const int32_t *index, int n, int key) {
   int lo = 0, hi = n;
   while (lo < hi) {

@@ -51,20 +51,10 @@ __global__ void __launch_bounds__(1024) eb_pr_kernel(EbArgs a) {
   const int stride = gridDim.x * a.workers_per_block;
 
   int32_t *win = pr_win + (size_t)(tid >> a.log2_team_lanes) * a.stage;
+  const int W = a.stage;
   for (int chunk = blockIdx.x * a.workers_per_block + wib; chunk < a.num_chunks; chunk += stride) {
-    const ChunkInfo ci = chunk_info<SEG>(a, chunk);
+    const ChunkInfo ci = SEG ? chunk_info<SEG>(a, chunk) : chunk_info_group(a, chunk, lane, tile, mask);
     if (blockIdx.y == 0 && cg == 0 && lane == 0) a.carry_rows[chunk] = ci.has_head ? ci.r_first : -1;
-    // stage the chunk's row starts when they fit the window
-    int nwin = 0;
-    if (!SEG && a.stage > 0) {
-      const int need = ci.r_last - ci.r_first + 2;
-      __syncwarp(mask);  // the previous chunk's searches are done
-      if (need <= a.stage) {
-        nwin = need;
-        for (int i = lane; i < need; i += tile) win[i] = __ldg(a.indptr + ci.r_first + i);
-      }
-      __syncwarp(mask);
-    }
 
     // running segment carried across steps; without a head row it starts as
     // the row before the chunk, so the first step zeroes the gap after it
@@ -73,6 +63,18 @@ __global__ void __launch_bounds__(1024) eb_pr_kernel(EbArgs a) {
     int run_cnt = 0;
     #pragma unroll
     for (int i = 0; i < V; i++) run[0][i] = ident;
+
+    // SpMM: a sliding window of row starts in shared memory, win[i] =
+    // indptr[min(win_base + i, M)], refilled from the current row whenever a
+    // step reaches past it; rows are searched there, not in global memory
+    int win_base = -1;
+    // the next step's column and value are loaded one step ahead
+    int c_next = 0;
+    float v_next = 0.f;
+    if (!SEG && ci.cs + lane < ci.ce) {
+      c_next = ld_idx(a.cols + ci.cs + lane, strm);
+      v_next = load_val<T>(vals, ci.cs + lane, strm);
+    }
 
     for (int sb = ci.cs; sb < ci.ce; sb += tile) {
       const int p = sb + lane;
@@ -83,21 +85,51 @@ __global__ void __launch_bounds__(1024) eb_pr_kernel(EbArgs a) {
       int cnt = 0;
       #pragma unroll
       for (int i = 0; i < V; i++) x[0][i] = ident;
+      int c = 0;
+      float v = 0.f;
+      float b[V];
+      if (SEG) {
+        c = p;
+        v = 1.f;
+      } else {
+        c = c_next;
+        v = v_next;
+        if ((unsigned)c >= (unsigned)a.K) { c = 0; v = 0.f; }
+        if (live && act[0]) load_vec<T, V>(B + (int64_t)c * a.N + col0, b, keep);
+        const int pn = p + tile;
+        if (pn < ci.ce) {
+          c_next = ld_idx(a.cols + pn, strm);
+          v_next = load_val<T>(vals, pn, strm);
+        }
+        // window: must hold the start of the step's last row's successor
+        const int plast = sb + nlive - 1;
+        const int rs = max(run_row, ci.r_first);  // row of nonzero sb is at least this
+        const bool stale = W > 0 && (win_base < 0 || rs < win_base ||
+                                     (win[W - 1] <= plast && win_base + W - 1 < a.M));
+        if (stale) {
+          __syncwarp(mask);
+          win_base = rs;
+          for (int i = lane; i < W; i += tile) win[i] = __ldg(a.indptr + min(win_base + i, a.M));
+          __syncwarp(mask);
+        }
+      }
       if (live) {
-        row = nwin ? win_row(win, nwin, ci.r_first, p) : chunk_row<SEG>(a, ci, p);
-        int c;
-        float v;
         if (SEG) {
-          c = p;
-          v = 1.f;
+          row = chunk_row<SEG>(a, ci, p);
+        } else if (W > 0 && (p < win[W - 1] || win_base + W - 1 >= a.M) && win[0] <= p) {
+          int lo = 1, hi = W - 1;  // first slot whose start is past p
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (win[mid] <= p) lo = mid + 1; else hi = mid;
+          }
+          row = min(win_base + hi - 1, ci.r_last);
         } else {
-          c = ld_idx(a.cols + p, strm);
-          v = load_val<T>(vals, p, strm);
-          if ((unsigned)c >= (unsigned)a.K) { c = 0; v = 0.f; }
+          row = chunk_row<SEG>(a, ci, p);
+        }
+        if (SEG) {
+          if (act[0]) load_vec<T, V>(B + (int64_t)c * a.N + col0, b, strm);
         }
         if (act[0]) {
-          float b[V];
-          load_vec<T, V>(B + (int64_t)c * a.N + col0, b, SEG ? strm : keep);
           #pragma unroll
           for (int i = 0; i < V; i++) x[0][i] = is_max ? b[i] : v * b[i];
         }

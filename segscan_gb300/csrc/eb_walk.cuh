@@ -121,27 +121,6 @@ __device__ __forceinline__ bool stage_wait(Stage &st, int b, unsigned mask, int 
   return ok;
 }
 
-// First r in [0, M] with indptr[r] >= key, found by all G lanes of the
-// group: each round every lane probes one of G split points of [lo, hi].
-__device__ __forceinline__ int group_lower_bound(const int32_t *indptr, int M, int key, int lane, int G,
-                                                 unsigned mask) {
-  int lo = 0, hi = M;  // answer in [lo, hi]
-  const unsigned lanes_bits = G >= 32 ? 0xffffffffu : ((1u << G) - 1u);
-  const unsigned shift = (threadIdx.x & 31u) & ~(unsigned)(G - 1);
-  while (lo < hi) {
-    const long long span = (long long)(hi - lo);
-    const int probe = lo + (int)((span * (lane + 1)) / (G + 1));
-    const bool ge = __ldg(indptr + probe) >= key;
-    const unsigned hits = (__ballot_sync(mask, ge) >> shift) & lanes_bits;
-    const int first = hits ? __ffs(hits) - 1 : G;  // first lane whose probe is >= key
-    const int nhi = first < G ? __shfl_sync(mask, probe, first, G) : hi;
-    const int nlo = first > 0 ? __shfl_sync(mask, probe, first - 1, G) + 1 : lo;
-    lo = nlo;
-    hi = nhi;
-  }
-  return lo;
-}
-
 template <int V, int NV, bool KAHAN>
 __device__ __forceinline__ void add_row(float (&acc)[NV][V], float (&comp)[NV][V], float v,
                                         const float (&b)[NV][V]) {
