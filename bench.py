@@ -452,7 +452,9 @@ def run_ours(args):
     wsz = api.spmm_workspace_size(Ad, N, strategy, knobs)
     work = torch.empty(wsz + 256, dtype=torch.uint8, device=dev) if wsz else None
     stream = torch.cuda.current_stream(dev)
-    kernels_per_step = 2 if strategy in ("ebsr", "ebpr") else 1
+    # ebsr: one walk launch (straddling rows assembled inside it, after a
+    # memset of the arrival counts); ebpr: scan + fix-up; row-balanced: one
+    kernels_per_step = 2 if strategy == "ebpr" else 1
 
     def step():
         api.spmm(Ad, Bd, strategy, knobs=knobs, out=C, workspace=work, stream=stream)
@@ -585,7 +587,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic_from_profiles(kernel_file),
-                     "kernel": f"{strategy} SpMM step (main kernel + carry fix-up)",
+                     "kernel": (f"{strategy} SpMM step (walk with in-kernel carry assembly)" if strategy == "ebsr"
+                                else f"{strategy} SpMM step"),
                      "bytes_per_launch": nbytes},
         "e2e": {"value": nbytes / t_e2e / 1e9 * ws_, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3, "pinned_copy_gbs": copy_gbs},

@@ -63,32 +63,19 @@ __global__ void __launch_bounds__(256) carry_fixup_kernel(const int32_t *__restr
   // launched as a programmatic dependent of the walk kernel: wait until the
   // walk's writes (head/tail slots, owner rows) are complete and visible
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  // a warp scans 32 consecutive chunks at once (one coalesced read of their
-  // head rows), then assembles the runs that lead there one after another
+  // one warp per chunk, so the runs are assembled in parallel; most chunks
+  // are not run leaders and return after two loads
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int c0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; c0 < num_chunks; c0 += warps * 32) {
-    const int c = c0 + lane;
-    bool lead = false;
-    if (c > 0 && c < num_chunks) {
-      const int r = rows[c];
-      lead = r >= 0 && r < M && rows[c - 1] != r;
-    }
-    unsigned leaders = __ballot_sync(0xffffffffu, lead);
-    while (leaders) {
-      const int l = __ffs(leaders) - 1;
-      leaders &= leaders - 1;
-      fixup_chunk<TC>(rows, heads, tails, num_chunks, N, M, C, reduce, accumulate, index, nnz, c0 + l, lane);
-    }
-  }
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_chunks; c += warps)
+    fixup_chunk<TC>(rows, heads, tails, num_chunks, N, M, C, reduce, accumulate, index, nnz, c, lane);
 }
 
 ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *C, int c_dtype,
                        int reduce, int accumulate, const int32_t *index, int nnz, cudaStream_t s) {
   if (num_chunks <= 1 || N == 0 || M == 0) return SS_OK;  // chunk 0 never carries
   const int threads = 256;
-  const int warps_needed = (num_chunks + 31) / 32;
-  const int blocks = std::max(1, std::min((warps_needed + 7) / 8, 152 * 8));
+  const int blocks = std::max(1, std::min((num_chunks + 7) / 8, 152 * 32));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks, 1, 1);
   cfg.blockDim = dim3(threads, 1, 1);

@@ -272,8 +272,19 @@ __device__ __forceinline__ void fixup_chunk(const int32_t *__restrict__ rows, co
   const int r = rows[c];
   if (c == 0 || r < 0 || r >= M) return;
   if (rows[c - 1] == r) return;  // not the leader of this run
+  // end of the run: the warp compares 32 head rows per step
   int cend = c + 1;
-  while (cend < num_chunks && rows[cend] == r) cend++;
+  while (true) {
+    const int k = cend + lane;
+    const bool same = k < num_chunks && rows[k] == r;
+    const unsigned m = __ballot_sync(0xffffffffu, same);
+    if (m == 0xffffffffu) {
+      cend += 32;
+    } else {
+      cend += __ffs(~m) - 1;
+      break;
+    }
+  }
   float count = 1.f;
   if (reduce == SS_MEAN && index != nullptr) {
     int lo = 0, hi = 0;
@@ -289,10 +300,16 @@ __device__ __forceinline__ void fixup_chunk(const int32_t *__restrict__ rows, co
   for (int j = lane; j < N; j += 32) {
     float acc = tails[(int64_t)(c - 1) * N + j];  // the owner's partial
     float comp = 0.f;
-    for (int k = c; k < cend; k++) {
-      const float x = heads[(int64_t)k * N + j];
-      if (reduce == SS_MAX) acc = fmaxf(acc, x);
-      else kahan_add(acc, comp, x);
+    for (int k0 = c; k0 < cend; k0 += 8) {  // eight heads in flight, added in order
+      float x[8];
+      #pragma unroll
+      for (int u = 0; u < 8; u++) x[u] = k0 + u < cend ? heads[(int64_t)(k0 + u) * N + j] : 0.f;
+      #pragma unroll
+      for (int u = 0; u < 8; u++) {
+        if (k0 + u >= cend) break;
+        if (reduce == SS_MAX) acc = fmaxf(acc, x[u]);
+        else kahan_add(acc, comp, x[u]);
+      }
     }
     if (accumulate) acc += Elem<TC>::to_f(crow[j]);
     if (reduce == SS_MEAN) acc = acc / count;

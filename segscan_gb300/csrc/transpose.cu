@@ -224,10 +224,25 @@ __global__ void __launch_bounds__(1024) sort_large_kernel(const int32_t *__restr
   }
 }
 
-// rowid[p] = row of nonzero p (binary_search_segment_number semantics)
+// rowid[p] = row of nonzero p (binary_search_segment_number semantics).
+// A thread takes ROWID_RUN consecutive nonzeros: one row search for the
+// first, then it walks indptr forward (rows only grow along p).
+constexpr int ROWID_RUN = 16;
 __global__ void rowid_kernel(const int32_t *__restrict__ indptr, int M, int nnz, int32_t *rowid) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nnz; p += (long long)gridDim.x * blockDim.x)
-    rowid[p] = row_search(indptr, 1, M, (int)p);
+  const long long runs = ((long long)nnz + ROWID_RUN - 1) / ROWID_RUN;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < runs; t += (long long)gridDim.x * blockDim.x) {
+    const int p0 = (int)(t * ROWID_RUN);
+    const int p1 = min(p0 + ROWID_RUN, nnz);
+    int r = row_search(indptr, 1, M, p0);
+    int next = __ldg(indptr + min(r + 1, M));
+    for (int p = p0; p < p1; p++) {
+      while (p >= next && r < M - 1) {
+        r++;
+        next = __ldg(indptr + r + 1);
+      }
+      rowid[p] = r;
+    }
+  }
 }
 
 __global__ void gather_rows_kernel(const int32_t *__restrict__ perm, const int32_t *__restrict__ rowid, int nnz,
@@ -283,7 +298,7 @@ ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indice
   e = cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_SORT_MAX * 4);
   if (e != cudaSuccess) return cuda_fail(e, "transpose sort attribute");
   sort_large_kernel<<<2 * 152, 1024, SMEM_SORT_MAX * 4, s>>>(t_indptr, perm, w.work);
-  rowid_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indptr, M, nnz, w.rowid);
+  rowid_kernel<<<grid_for((nnz + ROWID_RUN - 1) / ROWID_RUN, 256), 256, 0, s>>>(A->indptr, M, nnz, w.rowid);
   gather_rows_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(perm, w.rowid, nnz, t_indices);
   e = cudaGetLastError();
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
