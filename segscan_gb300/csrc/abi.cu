@@ -184,7 +184,7 @@ ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_byt
   // small thread_nz tuples then run as fast as tuned ones.
   const long long wave_groups = 152LL * 1024 / G;
   long long share = nnz > 0 ? ceil_div((long long)nnz, wave_groups) : 0;
-  share = ceil_div(share, 8LL * G) * 8LL * G;  // whole staged tiles keep the bulk copies aligned
+  share = ceil_div(share, 32LL) * 32;  // a multiple of 8 keeps the bulk copies 16-byte aligned
   if (share > g.chunk && share <= (1LL << 30)) g.chunk = (int)share;
   g.num_chunks = nnz > 0 ? ceil_div(nnz, g.chunk) : 0;
   // staged tile: 64 nonzeros, smaller when the block's groups would need
