@@ -400,7 +400,7 @@ def extra_fwd_bwd(dev, N=128):
     knobs32 = api.make_knobs("ebsr", N, group_factor=5, thread_nz=32, thread_per_block=512, block_denom=1)
     knobs16 = api.make_knobs("ebsr", N, group_factor=4, coarsen_factor=8, thread_nz=32, thread_per_block=512,
                              block_denom=1)
-    for name, dt in (("fp32", torch.float32), ("bf16", torch.bfloat16)):
+    def one(dt):
         knobs = knobs32 if dt == torch.float32 else knobs16
         Ad = api.CsrMatrix.from_host(A, dev, dt, values=False)
         vals = torch.from_numpy(A.values).to(dev).to(dt).requires_grad_(True)
@@ -418,8 +418,8 @@ def extra_fwd_bwd(dev, N=128):
         def fwd():
             autograd.spmm(Ad, vals.detach(), Bd.detach(), "ebsr", knobs, pattern=pat)
 
-        total = _event_ms(step, 5, stream)
-        f = _event_ms(fwd, 5, stream)
+        total = _event_ms(step, 5, stream, warm=3)
+        f = _event_ms(fwd, 5, stream, warm=3)
         # the backward's pieces, timed alone
         A_v = Ad.with_values(vals.detach())
         sd = _event_ms(lambda: api.sddmm(A_v, dC, Bd.detach()), 5, stream)
@@ -427,8 +427,14 @@ def extra_fwd_bwd(dev, N=128):
         AT_v = AT.with_values(api.gather_values(vals.detach().float(), perm))
         dB = torch.empty((A.ncol, N), device=dev)
         db = _event_ms(lambda: api.spmm(AT_v, dC, "ebsr", knobs=knobs32, out=dB), 5, stream)
-        res[name] = {"fwd_bwd_ms": total, "fwd_ms": f, "bwd_ms": total - f, "sddmm_ms": sd, "dB_spmm_ms": db,
-                     "transpose_build_ms": t_ms, "knobs_fwd": knobs.as_dict()}
+        return {"fwd_bwd_ms": total, "fwd_ms": f, "bwd_ms": total - f, "sddmm_ms": sd, "dB_spmm_ms": db,
+                "transpose_build_ms": t_ms, "knobs_fwd": knobs.as_dict()}
+
+    # each precision in its own scope, the allocator's cache emptied between,
+    # so one run's gigabyte-sized temporaries do not crowd the next
+    for name, dt in (("fp32", torch.float32), ("bf16", torch.bfloat16)):
+        torch.cuda.empty_cache()
+        res[name] = one(dt)
     return res
 
 

@@ -196,6 +196,33 @@ def test_deterministic(cuda):
         assert torch.equal(c1, c2), strategy
 
 
+def test_small_chunks_merge_to_the_wave_share(cuda):
+    """Element-balanced chunks below the one-wave share are merged up to it:
+    a tiny thread_nz and a thread_nz of exactly that share give the same
+    chunking, hence the same bits; a larger thread_nz is kept (different
+    chunking, same result within the FP32 tolerance)."""
+    from segscan_gb300 import api
+    csr = synth.powerlaw(200_000, 200_000, 2.1, 1, 20000, seed=31)
+    B = torch.from_numpy(synth.dense(csr.ncol, 64, seed=32)).cuda()
+    A = dev_csr(csr)
+    G = 16
+    share = -(-csr.nnz // (152 * 1024 // G))
+    share = -(-share // 32) * 32
+    assert share % G == 0
+    tiny = spmm(A, B, "ebsr", knobs=api.make_knobs("ebsr", 64, group_factor=4, thread_nz=1, block_denom=1))
+    exact = spmm(A, B, "ebsr", knobs=api.make_knobs("ebsr", 64, group_factor=4, thread_nz=share // G, block_denom=1))
+    assert torch.equal(tiny, exact)
+    big = spmm(A, B, "ebsr", knobs=api.make_knobs("ebsr", 64, group_factor=4, thread_nz=4 * share // G,
+                                                     block_denom=1))
+    C64, absC = oracle64(csr, B.cpu().numpy())
+    for C in (tiny, big):
+        check_close(C.cpu().numpy(), C64, absC, 1e-5, 1e-5, "merged chunks")
+    n_tiny = api.spmm_workspace_size(A, 64, "ebsr", api.make_knobs("ebsr", 64, group_factor=4, thread_nz=1))
+    n_exact = api.spmm_workspace_size(A, 64, "ebsr", api.make_knobs("ebsr", 64, group_factor=4,
+                                                                     thread_nz=share // G))
+    assert n_tiny == n_exact
+
+
 def test_row_ids_bit_exact(cuda):
     from segscan_gb300 import api
     g = np.load(GOLD / "row_ids_edge.npz")
