@@ -404,7 +404,7 @@ def extra_fwd_bwd(dev, N=128):
         knobs = knobs32 if dt == torch.float32 else knobs16
         Ad = api.CsrMatrix.from_host(A, dev, dt, values=False)
         vals = torch.from_numpy(A.values).to(dev).to(dt).requires_grad_(True)
-        Bd = B32.to(dt).requires_grad_(True)
+        Bd = B32.detach().to(dt, copy=True).requires_grad_(True)  # a fresh leaf for each precision
         pat = autograd.pattern(Ad)
         t_ms = _event_ms(lambda: api.transpose(Ad), 3, stream, warm=1)
         pat.transposed()
