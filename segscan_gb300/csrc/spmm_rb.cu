@@ -166,22 +166,28 @@ __device__ __forceinline__ void rbpr_slot(const RbArgs &a, int s, int e, int slo
   // together, then their four B rows, so a long row costs two dependent
   // round trips per four of its nonzeros on each slot
   constexpr int U = 4;
+  // the next step's columns and values are loaded while this step's B rows
+  // are in flight: one dependent round trip per step on a long row
+  int cn[U];
+  float vn[U];
+  #pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int p = s + slot + u * S;
+    cn[u] = -1;
+    vn[u] = 0.f;
+    if (p < e) {
+      cn[u] = ld_idx(a.indices + p, strm);
+      vn[u] = load_val<T>(vals, p, strm);
+    }
+  }
   for (int p0 = s + slot; p0 < e; p0 += U * S) {
     int c[U];
     float v[U];
     float b[U][NV][V];
     #pragma unroll
     for (int u = 0; u < U; u++) {
-      const int p = p0 + u * S;
-      c[u] = -1;
-      v[u] = 0.f;
-      if (p < e) {
-        c[u] = ld_idx(a.indices + p, strm);
-        v[u] = load_val<T>(vals, p, strm);
-      }
-    }
-    #pragma unroll
-    for (int u = 0; u < U; u++) {
+      c[u] = cn[u];
+      v[u] = vn[u];
       if ((unsigned)c[u] >= (unsigned)a.K) { c[u] = -1; v[u] = 0.f; }  // past the row, or a bad column
       #pragma unroll
       for (int j = 0; j < NV; j++) {
@@ -191,6 +197,16 @@ __device__ __forceinline__ void rbpr_slot(const RbArgs &a, int s, int e, int slo
           #pragma unroll
           for (int i = 0; i < V; i++) b[u][j][i] = 0.f;
         }
+      }
+    }
+    #pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int p = p0 + U * S + u * S;
+      cn[u] = -1;
+      vn[u] = 0.f;
+      if (p < e) {
+        cn[u] = ld_idx(a.indices + p, strm);
+        vn[u] = load_val<T>(vals, p, strm);
       }
     }
     #pragma unroll
