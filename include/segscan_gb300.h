@@ -152,7 +152,10 @@ ss_status ss_spmm_rbpr(const ss_csr *A, int N, const void *B, void *C,
 
 /* Replaces csrspmm_rowcaching_nnzbalance_cg<Index, DType, group_factor,
  * thread_per_block, CoarsenFactor, ThreadNz, block_numer, block_denom>
- * (spmm_cg.cuh:553-555). */
+ * (spmm_cg.cuh:553-555).  Chunks (ThreadNz * 2^group_factor nonzeros)
+ * smaller than the nonzeros' share per resident group of one full wave are
+ * merged up to that share (also for ebpr); the result is the same up to
+ * FP32 rounding order, deterministic for given inputs and knobs. */
 ss_status ss_spmm_ebsr(const ss_csr *A, int N, const void *B, void *C,
                        int c_dtype, int accumulate, const ss_knobs *knobs,
                        void *ws, size_t ws_bytes, void *stream);
@@ -255,7 +258,8 @@ ss_status ss_index_validate(const int32_t *index, int nnz, int dst_len,
  * coarsen_factor and thread_per_block come from per_mat[0] (NULL = ebsr
  * defaults).  ss_batch_plan uploads the plan and synchronises the stream.
  * ss_spmm_batched then computes C[m] = A[m] * B[m] for every m in one
- * persistent launch plus one fix-up launch, stream-ordered (it can be
+ * persistent launch (after one memset of its counters; rows that straddle
+ * work items are assembled inside that launch), stream-ordered (it can be
  * replayed from a captured CUDA graph).  Not in the reference. */
 ss_status ss_batch_plan_size(int count, const ss_csr *mats, int N,
                              const ss_knobs *per_mat, size_t *host_bytes,

@@ -1,8 +1,8 @@
 """Batched SpMM: many independent CSR matrices in one persistent launch.
 
 The C ABI builds a device plan of (matrix, chunk) work items
-(ss_batch_plan) and runs it in one persistent walk launch plus one fix-up
-launch (ss_spmm_batched).  This module holds the plan, the outputs and an
+(ss_batch_plan) and runs it in one persistent walk launch, which also
+assembles the rows that straddle work items (ss_spmm_batched).  This module holds the plan, the outputs and an
 optional CUDA graph of the step, and chooses each matrix's chunk size from
 its row-length statistics (see autotune.batch_knobs).  The reference has no
 batched mode; its drivers launch one matrix at a time.

@@ -6,8 +6,10 @@
 // stores when the row also ends in that chunk.  Only two rows of a chunk can
 // straddle a chunk boundary: the HEAD row (started in an earlier chunk) and
 // the last row (continues into the next chunk).  Their FP32 partials go to
-// the chunk's head and tail slots, and a fix-up pass assembles each
-// straddling row as owner tail + following heads and stores it once, so a
+// the chunk's head and tail slots, and each straddling row is assembled
+// once as owner tail + following heads (by the last of its chunks to finish,
+// carry_arrive, in the ebsr and batched walks; by the fix-up kernel,
+// fixup_chunk, after the ebpr and segment kernels) and stored once, so a
 // 16-bit output is rounded once.  Empty rows (empty
 // segments) are written as zero by the chunk holding the next nonzero, so in
 // overwrite mode every output row is written exactly once, no zero fill and

@@ -17,9 +17,10 @@
 //    same A, N and knobs) is larger is rejected with SS_ERR_CAPACITY;
 //  * all calls on a device share the one array.  Calls that overlap on the
 //    GPU (different streams, or host threads that do not order them) race on
-//    it; serialise them.  Nothing in the array needs clearing between calls:
-//    the kernels write every carry slot before the fix-up reads it, so the
-//    previous call's contents are never used;
+//    it; serialise them.  Nothing in the array needs clearing by the
+//    caller: the call zeroes its arrival counts itself (stream-ordered) and
+//    the walk writes every carry slot before it is read, so the previous
+//    call's contents are never used;
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
 //    before any stream capture.
