@@ -119,6 +119,12 @@ const char *ss_last_error(void);
  * resets it.  Synchronous with respect to the device.  No counterpart in the
  * reference (its kernels never wait). */
 ss_status ss_device_error(int *status, int clear);
+/* Diagnostic: one bounded mbarrier wait that can never complete (an
+ * expected transaction no copy delivers) gives up after `polls` tries and
+ * sets the device flag above to SS_ERR_TIMEOUT, the path a lost bulk copy
+ * takes in the walk kernels; the context stays usable.  No counterpart in
+ * the reference. */
+ss_status ss_selftest_bounded_wait(int polls, void *stream);
 /* L2 budget (bytes) for the gathered dense operand B: when B is larger,
  * only a fixed address subset of that size is marked evict_last and the
  * rest evict_first, so the kept subset stays resident.  0 (the default)

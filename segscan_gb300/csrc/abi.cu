@@ -393,6 +393,7 @@ ss_status ss_spmm_workspace_size(int strategy, const ss_csr *A, int N, const ss_
 
 ss_status ss_spmm(int strategy, const ss_csr *A, int N, const void *B, void *C, int c_dtype, int accumulate,
                   const ss_knobs *knobs, void *ws, size_t ws_bytes, void *stream) {
+  ss::NvtxRange nvtx_range("ss_spmm");
   ss_knobs tmp;
   const ss_knobs *k = knobs_or_default(strategy, N, knobs, tmp);
   SpmmCall c;
@@ -476,6 +477,7 @@ ss_status ss_segment_coo_workspace_size(int seg_strategy, int nnz, int N, const 
 ss_status ss_segment_coo(int seg_strategy, const void *src, int src_dtype, const int32_t *index, int nnz, int N,
                          int dst_len, float *dst, int reduce, int accumulate, const ss_knobs *knobs, void *ws,
                          size_t ws_bytes, void *stream) {
+  ss::NvtxRange nvtx_range("ss_segment_coo");
   if (nnz < 0 || N < 0 || dst_len < 0) return fail(SS_ERR_INVALID_ARG, "negative size");
   if (src_dtype < SS_F32 || src_dtype > SS_F16) return fail(SS_ERR_INVALID_ARG, "src_dtype %d unknown", src_dtype);
   if (reduce < SS_SUM || reduce > SS_MEAN) return fail(SS_ERR_INVALID_ARG, "reduce %d unknown", reduce);

@@ -146,6 +146,7 @@ ss_status ss_batch_plan(int count, const ss_csr *mats, int N, const void *const 
 }
 
 ss_status ss_spmm_batched(const void *host_plan, void *dev_plan, void *stream) {
+  ss::NvtxRange nvtx_range("ss_spmm_batched");
   if (!host_plan || !dev_plan) return fail(SS_ERR_INVALID_ARG, "null plan");
   BatchHeader h;
   memcpy(&h, host_plan, sizeof(h));

@@ -111,3 +111,35 @@ extern "C" ss_status ss_device_error(int *status, int clear) {
   *status = v;
   return SS_OK;
 }
+
+namespace ss {
+
+// One bounded wait that can never complete: an mbarrier expecting 16 bytes
+// of transaction that no copy will deliver.  The wait gives up after
+// `polls` tries and records SS_ERR_TIMEOUT in the flag the walk kernels use,
+// the path a lost bulk copy would take, without any fault.
+__global__ void bounded_wait_selftest_kernel(int polls, int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_expect_tx(&bar, 16);
+  for (int it = 0; !mbar_try_wait(&bar, 0); ) {
+    if (++it >= polls) {
+      if (err) atomicExch(err, (int)SS_ERR_TIMEOUT);
+      break;
+    }
+  }
+}
+
+}  // namespace ss
+
+extern "C" ss_status ss_selftest_bounded_wait(int polls, void *stream) {
+  if (polls < 1 || polls > (1 << 22)) return ss::fail(SS_ERR_INVALID_ARG, "polls %d outside [1, 2^22]", polls);
+  int *err = ss::walk_error_ptr();
+  if (!err) return ss::fail(SS_ERR_CUDA, "device error flag unavailable");
+  ss::bounded_wait_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(polls, err);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SS_OK : ss::cuda_fail(e, "bounded-wait self-test launch");
+}
+

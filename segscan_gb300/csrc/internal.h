@@ -5,9 +5,20 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/segscan_gb300.h"
 
 namespace ss {
+
+// NVTX range around one library call (shows the entry point on a profiler
+// timeline; a no-op unless a tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Records a failure message for ss_last_error() and returns `st`.
 ss_status fail(ss_status st, const char *fmt, ...);

@@ -76,6 +76,7 @@ static void *sddmm_ptr(int V) {
 using namespace ss;
 
 extern "C" ss_status ss_sddmm(const ss_csr *A, int N, const float *dC, const void *B, float *dvals, void *stream) {
+  ss::NvtxRange nvtx_range("ss_sddmm");
   if (!A || A->nrow < 0 || A->ncol < 0 || A->nnz < 0 || N < 0) return fail(SS_ERR_INVALID_ARG, "bad arguments");
   if (A->value_dtype < SS_F32 || A->value_dtype > SS_F16) return fail(SS_ERR_INVALID_ARG, "bad dtype");
   const int nnz = A->nnz;

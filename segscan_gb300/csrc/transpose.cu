@@ -268,6 +268,7 @@ ss_status ss_csr_transpose_workspace_size(const ss_csr *A, size_t *bytes) {
 
 ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indices, int32_t *perm, void *ws,
                            size_t ws_bytes, void *stream) {
+  ss::NvtxRange nvtx_range("ss_csr_transpose");
   if (!A || A->nrow < 0 || A->ncol < 0 || A->nnz < 0) return fail(SS_ERR_INVALID_ARG, "bad CSR descriptor");
   const int M = A->nrow, K = A->ncol, nnz = A->nnz;
   if (!t_indptr || (nnz > 0 && (!t_indices || !perm || !A->indices || !A->indptr)))

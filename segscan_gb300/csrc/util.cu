@@ -64,6 +64,7 @@ extern "C" {
 
 ss_status ss_row_ids(const int32_t *indptr, int M, int nnz, const int32_t *elems, int64_t count, int32_t *rows,
                      void *stream) {
+  ss::NvtxRange nvtx_range("ss_row_ids");
   if (M < 1 || nnz < 0 || count < 0) return fail(SS_ERR_INVALID_ARG, "bad sizes (M %d nnz %d)", M, nnz);
   if (count == 0) return SS_OK;
   if (!indptr || !rows) return fail(SS_ERR_INVALID_ARG, "null pointer");
