@@ -26,7 +26,9 @@
  *    With accumulate = 1 the result is added (C += A*B), matching the
  *    reference launchers whose callers pre-zero C.
  *  - Values and B share one storage type (SS_F32, SS_BF16 or SS_F16);
- *    arithmetic is FP32 in every kernel; C is FP32 or the storage type.
+ *    arithmetic is FP32 in every kernel; C is FP32 or the storage type
+ *    (ebsr with FP32 storage also writes a BF16/FP16 C, rounding in its
+ *    stores).
  */
 #ifndef SEGSCAN_GB300_H
 #define SEGSCAN_GB300_H

@@ -9,7 +9,8 @@ Backward:
                                      stable counting-sort transpose once per
                                      pattern and cached)
 Values stored in BF16/FP16 get FP32 gradients cast back to their dtype;
-dB is computed in FP32 (A^T values widened to FP32) and cast to B's dtype.
+dB is computed in FP32 (A^T values widened to FP32) and rounded to B's dtype
+by the ebsr walk's own stores (other strategies: a cast after).
 This module is the training / test binding only; the library is the C ABI.
 """
 from __future__ import annotations
@@ -57,7 +58,12 @@ class SpMMFunction(torch.autograd.Function):
         if ctx.needs_input_grad[1]:
             AT, perm = pattern.transposed()
             t_vals = api.gather_values(values.float().contiguous(), perm)
-            d_B = api.spmm(AT.with_values(t_vals), dC, ctx.bw_strategy, knobs=ctx.bw_knobs).to(B.dtype)
+            AT_v = AT.with_values(t_vals)
+            if ctx.bw_strategy == "ebsr" and B.dtype != torch.float32:
+                # the walk rounds its FP32 sums straight into B's 16-bit type
+                d_B = api.spmm(AT_v, dC, "ebsr", knobs=ctx.bw_knobs, out_dtype=B.dtype)
+            else:
+                d_B = api.spmm(AT_v, dC, ctx.bw_strategy, knobs=ctx.bw_knobs).to(B.dtype)
         return d_values, d_B, None, None, None, None, None
 
 

@@ -276,13 +276,17 @@ static const ss_knobs *knobs_or_default(int strategy, int N, const ss_knobs *k, 
   return &tmp;
 }
 
-static ss_status make_spmm_call(const ss_csr *A, int N, const void *B, void *C, int c_dtype, int accumulate,
-                                const ss_knobs &k, SpmmCall &c) {
+static ss_status make_spmm_call(int strategy, const ss_csr *A, int N, const void *B, void *C, int c_dtype,
+                                int accumulate, const ss_knobs &k, SpmmCall &c) {
   ss_status st = check_csr(A, N);
   if (st) return st;
   if (A->nrow > 0 && N > 0 && !C) return fail(SS_ERR_INVALID_ARG, "C is null");
   if (A->nnz > 0 && N > 0 && !B) return fail(SS_ERR_INVALID_ARG, "B is null");
-  if (c_dtype != SS_F32 && c_dtype != A->value_dtype)
+  // C is FP32 or the value type; ebsr with FP32 values also writes BF16/FP16
+  // C directly (its stores round the FP32 sums)
+  const bool c16_from_f32 = strategy == SS_EBSR && A->value_dtype == SS_F32 &&
+                            (c_dtype == SS_BF16 || c_dtype == SS_F16);
+  if (c_dtype != SS_F32 && c_dtype != A->value_dtype && !c16_from_f32)
     return fail(SS_ERR_INVALID_ARG, "c_dtype %d must be SS_F32 or the value dtype", c_dtype);
   if (accumulate != 0 && accumulate != 1) return fail(SS_ERR_INVALID_ARG, "accumulate must be 0 or 1");
   const int es = dtype_size(A->value_dtype);
@@ -397,7 +401,7 @@ ss_status ss_spmm(int strategy, const ss_csr *A, int N, const void *B, void *C, 
   ss_knobs tmp;
   const ss_knobs *k = knobs_or_default(strategy, N, knobs, tmp);
   SpmmCall c;
-  ss_status st = make_spmm_call(A, N, B, C, c_dtype, accumulate, *k, c);
+  ss_status st = make_spmm_call(strategy, A, N, B, C, c_dtype, accumulate, *k, c);
   if (st) return st;
   RbGeom rg;
   EbGeom eg;

@@ -67,7 +67,8 @@ ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
   a.use_tma = aligned16(c.indices) && (c.vals == nullptr || aligned16(c.vals)) && (g.chunk % 8) == 0;
   a.err = walk_error_ptr();
   void *fn = nullptr;
-  if (c.val_dtype == SS_F32) fn = sr_kernel_f32(g.cs.V, g.cs.NV, false);
+  if (c.val_dtype == SS_F32)
+    fn = c.c_dtype == SS_F32 ? sr_kernel_f32(g.cs.V, g.cs.NV, false) : sr_kernel_f32_c16(g.cs.V, g.cs.NV, c.c_dtype);
   else if (c.val_dtype == SS_BF16) fn = sr_kernel_bf16(g.cs.V, g.cs.NV, false, c.c_dtype == SS_F32);
   else fn = sr_kernel_f16(g.cs.V, g.cs.NV, false, c.c_dtype == SS_F32);
   // straddling rows are assembled inside the walk (carry_arrive): only the

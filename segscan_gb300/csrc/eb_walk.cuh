@@ -576,6 +576,7 @@ inline void *sr_ptr(int V, int NV) {
 
 // Kernel tables, one translation unit per storage type (eb_walk_*.cu).
 void *sr_kernel_f32(int V, int NV, bool seg);
+void *sr_kernel_f32_c16(int V, int NV, int c_dtype);  // FP32 inputs, BF16/FP16 C (SpMM)
 void *sr_kernel_bf16(int V, int NV, bool seg, bool out_f32);
 void *sr_kernel_f16(int V, int NV, bool seg, bool out_f32);
 

@@ -126,6 +126,35 @@ def test_half_storage(cuda, strategy, dtype, out_f32):
     assert np.all(err <= bound), f"{strategy} {dtype}: worst {np.max(err - bound):.3e} over the bound"
 
 
+@pytest.mark.parametrize("out_dtype", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("accumulate", [False, True])
+def test_f32_inputs_16bit_output(cuda, out_dtype, accumulate):
+    """ebsr with FP32 values and B writes a BF16/FP16 C directly: FP32 sums
+    (and, accumulating, the old C added in FP32), rounded once to the output
+    type; other strategies refuse the combination."""
+    from segscan_gb300 import api
+    csr = powerlaw_medium(M=20000, lmax=3000)
+    B = synth.dense(csr.ncol, 64, seed=12)
+    A = dev_csr(csr)
+    Bd = torch.from_numpy(B).cuda()
+    old = torch.from_numpy(synth.dense(csr.nrow, 64, seed=13)).cuda().to(out_dtype)
+    C = old.clone()
+    api.spmm(A, Bd, "ebsr", out=C, accumulate=accumulate)
+    torch.cuda.synchronize()
+    C64, absC = oracle64(csr, B)
+    if accumulate:
+        prev = old.double().cpu().numpy()
+        C64, absC = C64 + prev, absC + np.abs(prev)
+    u = 2.0 ** -8 if out_dtype == torch.bfloat16 else 2.0 ** -11
+    atol = F16_ATOL if out_dtype == torch.float16 else 1e-30
+    err = np.abs(C.double().cpu().numpy() - C64)
+    bound = np.abs(C64) * u + 1e-5 * absC + atol
+    assert np.all(err <= bound), f"{out_dtype}: worst {np.max(err - bound):.3e} over the bound"
+    for strategy in ("ebpr", "rbpr", "rbsr"):
+        with pytest.raises(Exception):
+            api.spmm(A, Bd, strategy, out_dtype=out_dtype)
+
+
 @pytest.mark.parametrize("strategy", STRATS)
 def test_accumulate(cuda, strategy):
     csr = synth.poisson(300, 300, 5.0, seed=4)
