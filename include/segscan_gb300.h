@@ -254,6 +254,27 @@ ss_status ss_index_validate(const int32_t *index, int nnz, int dst_len,
                             int32_t *d_flag, void *stream);
 
 /* ---------------------------------------------------------------- */
+/* Matrix Market input (host side).                                   */
+/* ---------------------------------------------------------------- */
+
+/* Replaces read_mtx_file (test-cg/include/dataloader/dataloader.hpp:22-107):
+ * a coordinate file's pattern as CSR (values dropped; pass values = NULL to
+ * the SpMM calls for ones, as the reference's descriptor does), symmetric
+ * files expanded and de-duplicated, entries sorted by (row, column).
+ * SS_MTX_REFERENCE gives the reference's result exactly, including its CSR
+ * build stopping after the file's declared entry count (an expanded
+ * symmetric file loses its last rows' entries there); SS_MTX_FULL keeps every
+ * entry and also expands skew-symmetric and hermitian files.  Errors are
+ * status codes (the reference exit()s).  ss_mtx_shape then ss_mtx_csr copy
+ * the result into caller buffers of nrow + 1 and nnz int32. */
+typedef struct ss_mtx ss_mtx;
+enum { SS_MTX_REFERENCE = 0, SS_MTX_FULL = 1 };
+ss_status ss_mtx_read(const char *path, int mode, ss_mtx **out);
+ss_status ss_mtx_shape(const ss_mtx *m, int *nrow, int *ncol, int *nnz);
+ss_status ss_mtx_csr(const ss_mtx *m, int32_t *indptr, int32_t *indices);
+void ss_mtx_free(ss_mtx *m);
+
+/* ---------------------------------------------------------------- */
 /* Batched SpMM: many independent CSR matrices in one persistent launch */
 /* ---------------------------------------------------------------- */
 

@@ -58,4 +58,21 @@ void ref_transpose(int nrow, int ncol, int nnz, const int *coo_row,
   (void)nrow;
 }
 
+// read_mtx_file (dataloader.hpp:22-107): the reference's Matrix Market
+// reader, pattern only.  First call with null outputs to get the sizes
+// (nrow, ncol, nnz after its own processing), then with buffers of
+// nrow + 1 and nnz entries.  Valid files only (the reference exit()s).
+void ref_read_mtx(const char *path, int *nrow, int *ncol, int *nnz, int *indptr, int *indices) {
+  int M = 0, K = 0, Z = 0;
+  std::vector<int> ip, ix, coo;
+  read_mtx_file(path, M, K, Z, ip, ix, coo);
+  *nrow = M;
+  *ncol = K;
+  *nnz = Z;
+  if (indptr)
+    for (size_t i = 0; i < ip.size(); i++) indptr[i] = ip[i];
+  if (indices)
+    for (size_t i = 0; i < ix.size(); i++) indices[i] = ix[i];
+}
+
 }  // extern "C"

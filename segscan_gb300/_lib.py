@@ -80,6 +80,10 @@ _SIGNATURES = {
     "ss_default_knobs": (c_int, [c_int, c_int, POINTER(SsKnobs)]),
     "ss_device_error": (c_int, [POINTER(c_int), c_int]),
     "ss_selftest_bounded_wait": (c_int, [c_int, c_void_p]),
+    "ss_mtx_read": (c_int, [c_char_p, c_int, POINTER(c_void_p)]),
+    "ss_mtx_shape": (c_int, [c_void_p, POINTER(c_int), POINTER(c_int), POINTER(c_int)]),
+    "ss_mtx_csr": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "ss_mtx_free": (None, [c_void_p]),
     "ss_set_l2_keep_bytes": (c_int, [ctypes.c_longlong]),
     "ss_spmm_workspace_size": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(SsKnobs), POINTER(c_size_t)]),
     "ss_spmm_ebpr": (c_int, [POINTER(SsCsr), c_int, c_void_p, c_void_p, c_int, c_int, POINTER(SsKnobs),

@@ -6,6 +6,7 @@ reference sources into oracle/_ref/libsegscan_ref.so:
   binary_search_segment_number     test-cg/include/util/check.cuh:88-102
   transpose + compressedRow        test-cg/include/dataloader/dataloader.hpp:109-144
   segment_coo_sequencial           new-cg/include/utils/check.cuh:44-52
+  read_mtx_file                    test-cg/include/dataloader/dataloader.hpp:22-107
 
 Run it where the reference checkout exists:
     python tests/golden/make_golden.py [--ref /path/to/segScan]
@@ -130,6 +131,23 @@ def main() -> None:
     dst_len = E.nrow + 2
     np.savez_compressed(HERE / "segment_edge_n5.npz", index=index, src=src, dst_len=dst_len,
                         dst=ref_segment(lib, src, index, dst_len))
+    # 7. Matrix Market files (tests/mtx_cases.py) read by the reference's
+    #    loader; the .mtx texts are committed beside the expected CSR.
+    sys.path.insert(0, str(HERE.parent))
+    import mtx_cases
+    expect = {}
+    for case in mtx_cases.CASES:
+        path = HERE / f"mtx_{case}.mtx"
+        mtx_cases.write(path, case)
+        M, K, Z = c_int(), c_int(), c_int()
+        lib.ref_read_mtx(str(path).encode(), ctypes.byref(M), ctypes.byref(K), ctypes.byref(Z), None, None)
+        ip = np.empty(M.value + 1, np.int32)
+        ix = np.empty(max(Z.value, 1), np.int32)
+        lib.ref_read_mtx(str(path).encode(), ctypes.byref(M), ctypes.byref(K), ctypes.byref(Z), _p(ip), _p(ix))
+        expect[f"{case}_shape"] = np.array([M.value, K.value, Z.value], np.int64)
+        expect[f"{case}_indptr"] = ip
+        expect[f"{case}_indices"] = ix[:Z.value]
+    np.savez_compressed(HERE / "mtx_reference.npz", **expect)
     for f in sorted(HERE.glob("*.npz")):
         print(f"{f.name}: {f.stat().st_size} bytes")
 
