@@ -236,6 +236,20 @@ ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr,
                            int32_t *t_indices, int32_t *perm, void *ws,
                            size_t ws_bytes, void *stream);
 
+/* COO -> CSR on the device, the counterpart of compressedRow
+ * (test-cg/include/dataloader/dataloader.hpp:109-121), which assumes its
+ * input sorted by row: here any order is accepted and the result is the
+ * stable counting sort by row (entries of a row keep their input order).
+ * indptr [nrow + 1], out_cols [nnz], perm [nnz] (perm[q] = input position
+ * of entry q; pass it to ss_gather_values for the values).  Rows outside
+ * [0, nrow) are left out (they land past indptr[nrow]).  Workspace from
+ * ss_coo_to_csr_workspace_size. */
+ss_status ss_coo_to_csr_workspace_size(int nrow, int nnz, size_t *bytes);
+ss_status ss_coo_to_csr(int nrow, int nnz, const int32_t *rows,
+                        const int32_t *cols, int32_t *indptr,
+                        int32_t *out_cols, int32_t *perm, void *ws,
+                        size_t ws_bytes, void *stream);
+
 /* out[p] = perm-gathered values: out[q] = values[perm[q]] (any dtype). */
 ss_status ss_gather_values(const void *values, int dtype, const int32_t *perm,
                            int nnz, void *out, void *stream);

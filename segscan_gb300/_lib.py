@@ -80,6 +80,9 @@ _SIGNATURES = {
     "ss_default_knobs": (c_int, [c_int, c_int, POINTER(SsKnobs)]),
     "ss_device_error": (c_int, [POINTER(c_int), c_int]),
     "ss_selftest_bounded_wait": (c_int, [c_int, c_void_p]),
+    "ss_coo_to_csr_workspace_size": (c_int, [c_int, c_int, POINTER(c_size_t)]),
+    "ss_coo_to_csr": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                              c_void_p]),
     "ss_mtx_read": (c_int, [c_char_p, c_int, POINTER(c_void_p)]),
     "ss_mtx_shape": (c_int, [c_void_p, POINTER(c_int), POINTER(c_int), POINTER(c_int)]),
     "ss_mtx_csr": (c_int, [c_void_p, c_void_p, c_void_p]),

@@ -333,6 +333,31 @@ def transpose(A: CsrMatrix, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
     return CsrMatrix(A.ncol, A.nrow, t_indptr, t_indices, vals), perm
 
 
+def coo_to_csr(nrow: int, rows: torch.Tensor, cols: torch.Tensor, ncol: Optional[int] = None,
+               values: Optional[torch.Tensor] = None, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
+    """(CSR matrix, perm) from COO rows/cols on the device: a stable counting
+    sort by row (compressedRow, dataloader.hpp:109-121, for sorted input);
+    values, if given, are gathered along."""
+    _need_cuda("rows", rows, torch.int32)
+    _need_cuda("cols", cols, torch.int32)
+    nnz = int(rows.numel())
+    if cols.numel() != nnz:
+        raise ValueError("rows and cols differ in length")
+    dev = rows.device
+    n = ctypes.c_size_t()
+    _lib.call("ss_coo_to_csr_workspace_size", nrow, nnz, ctypes.byref(n))
+    ws = _workspace(int(n.value), dev)  # held until the launches are queued: the
+    wp, wn = _aligned(ws)                # allocator must not hand it to the outputs below
+    indptr = torch.empty(nrow + 1, dtype=torch.int32, device=dev)
+    out_cols = torch.empty(nnz, dtype=torch.int32, device=dev)
+    perm = torch.empty(nnz, dtype=torch.int32, device=dev)
+    _lib.call("ss_coo_to_csr", nrow, nnz, _ptr(rows), _ptr(cols), _ptr(indptr), _ptr(out_cols), _ptr(perm), wp, wn,
+              _stream(stream))
+    vals = gather_values(values, perm, stream) if values is not None else None
+    K = int(ncol) if ncol is not None else (int(cols.max()) + 1 if nnz else 0)
+    return CsrMatrix(nrow, K, indptr, out_cols, vals), perm
+
+
 def gather_values(values: torch.Tensor, perm: torch.Tensor, stream=None) -> torch.Tensor:
     _need_cuda("values", values)
     _need_cuda("perm", perm, torch.int32)

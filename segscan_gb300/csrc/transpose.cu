@@ -254,6 +254,37 @@ __global__ void gather_rows_kernel(const int32_t *__restrict__ perm, const int32
   }
 }
 
+// Steps 1-4: a stable counting sort of the positions [0, nnz) by key
+// (keys outside [0, K) are left out): out_indptr [K + 1] gets each key's
+// start, perm the positions grouped by key, ascending within a key.
+static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out_indptr, int32_t *perm,
+                               const TransposeWs &w, cudaStream_t s) {
+  const long long tiles = ((long long)K + SCAN_TILE - 1) / SCAN_TILE;
+  cudaError_t e = cudaMemsetAsync(w.counts, 0, (size_t)(K + 1) * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.work, 0, 4, s);
+  if (e != cudaSuccess) return cuda_fail(e, "counting sort clear");
+  if (K == 0) {  // no keys: out_indptr = [0]
+    e = cudaMemsetAsync(out_indptr, 0, 4, s);
+    return e == cudaSuccess ? SS_OK : cuda_fail(e, "counting sort clear");
+  }
+  if (nnz > 0) hist_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(keys, nnz, K, w.counts);
+  scan_tile_kernel<<<(int)tiles, 1024, 0, s>>>(w.counts, K, out_indptr, w.bsum);
+  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, (int)tiles, out_indptr + K);
+  scan_add_kernel<<<grid_for(K, 256), 256, 0, s>>>(out_indptr, K, w.bsum);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "counting sort scan");
+  if (nnz == 0) return SS_OK;
+  e = cudaMemcpyAsync(w.cursor, out_indptr, (size_t)K * 4, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "counting sort cursor");
+  scatter_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(keys, nnz, K, w.cursor, perm);
+  sort_small_kernel<<<grid_for(K, 256), 256, 0, s>>>(out_indptr, K, perm, w.work);
+  e = cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_SORT_MAX * 4);
+  if (e != cudaSuccess) return cuda_fail(e, "counting sort attribute");
+  sort_large_kernel<<<2 * 152, 1024, SMEM_SORT_MAX * 4, s>>>(out_indptr, perm, w.work);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SS_OK : cuda_fail(e, "counting sort launch");
+}
+
 }  // namespace ss
 
 using namespace ss;
@@ -281,28 +312,38 @@ ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indice
   TransposeWs w;
   transpose_ws_bytes(K, nnz, &w, ws);
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(w.counts, 0, (size_t)(K + 1) * 4, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.work, 0, 4, s);
-  if (e != cudaSuccess) return cuda_fail(e, "transpose clear");
-  if (K == 0) return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose");
-  if (nnz > 0) hist_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indices, nnz, K, w.counts);
-  scan_tile_kernel<<<(int)tiles, 1024, 0, s>>>(w.counts, K, t_indptr, w.bsum);
-  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, (int)tiles, t_indptr + K);
-  scan_add_kernel<<<grid_for(K, 256), 256, 0, s>>>(t_indptr, K, w.bsum);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "transpose scan");
-  if (nnz == 0) return SS_OK;
-  e = cudaMemcpyAsync(w.cursor, t_indptr, (size_t)K * 4, cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "transpose cursor");
-  scatter_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(A->indices, nnz, K, w.cursor, perm);
-  sort_small_kernel<<<grid_for(K, 256), 256, 0, s>>>(t_indptr, K, perm, w.work);
-  e = cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_SORT_MAX * 4);
-  if (e != cudaSuccess) return cuda_fail(e, "transpose sort attribute");
-  sort_large_kernel<<<2 * 152, 1024, SMEM_SORT_MAX * 4, s>>>(t_indptr, perm, w.work);
+  ss_status st = counting_sort(A->indices, nnz, K, t_indptr, perm, w, s);
+  if (st != SS_OK || nnz == 0 || K == 0) return st;
   rowid_kernel<<<grid_for((nnz + ROWID_RUN - 1) / ROWID_RUN, 256), 256, 0, s>>>(A->indptr, M, nnz, w.rowid);
   gather_rows_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(perm, w.rowid, nnz, t_indices);
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
+}
+
+ss_status ss_coo_to_csr_workspace_size(int nrow, int nnz, size_t *bytes) {
+  if (!bytes || nrow < 0 || nnz < 0) return fail(SS_ERR_INVALID_ARG, "bad arguments");
+  *bytes = transpose_ws_bytes(nrow, nnz, nullptr, nullptr);
+  return SS_OK;
+}
+
+ss_status ss_coo_to_csr(int nrow, int nnz, const int32_t *rows, const int32_t *cols, int32_t *indptr,
+                        int32_t *out_cols, int32_t *perm, void *ws, size_t ws_bytes, void *stream) {
+  ss::NvtxRange nvtx_range("ss_coo_to_csr");
+  if (nrow < 0 || nnz < 0 || !indptr || (nnz > 0 && (!rows || !cols || !out_cols || !perm)))
+    return fail(SS_ERR_INVALID_ARG, "bad arguments");
+  const long long tiles = ((long long)nrow + SCAN_TILE - 1) / SCAN_TILE;
+  if (tiles > SCAN_TILE) return fail(SS_ERR_CAPACITY, "nrow %d above the scan capacity %d", nrow, SCAN_TILE * SCAN_TILE);
+  const size_t need = transpose_ws_bytes(nrow, nnz, nullptr, nullptr);
+  if (ws_bytes < need || !ws || ((uintptr_t)ws % 256))
+    return fail(SS_ERR_WORKSPACE, "workspace needs %zu bytes (256-byte aligned), got %zu", need, ws_bytes);
+  TransposeWs w;
+  transpose_ws_bytes(nrow, nnz, &w, ws);
+  cudaStream_t s = (cudaStream_t)stream;
+  ss_status st = counting_sort(rows, nnz, nrow, indptr, perm, w, s);
+  if (st != SS_OK || nnz == 0 || nrow == 0) return st;
+  gather_rows_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(perm, cols, nnz, out_cols);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SS_OK : cuda_fail(e, "coo to csr launch");
 }
 
 }  // extern "C"

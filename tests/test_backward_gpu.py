@@ -160,3 +160,37 @@ def test_autograd_dense_reference(cuda, dtype):
     sv = (np.abs(W64) @ np.abs(B64.T))[rows, csr.indices]
     assert np.all(np.abs(Bd.grad.float().cpu().numpy() - gB_ref) <= tol * (sB + np.abs(gB_ref)) + 1e-12)
     assert np.all(np.abs(vals.grad.float().cpu().numpy() - gv_ref) <= tol * (sv + np.abs(gv_ref)) + 1e-12)
+
+
+@pytest.mark.parametrize("case", ["sorted", "shuffled", "skewed", "out_of_range", "empty"])
+def test_coo_to_csr(cuda, case):
+    """Device COO -> CSR: the stable counting sort by row (compressedRow,
+    dataloader.hpp:109-121, on sorted input), bit for bit against numpy's
+    stable argsort; rows outside [0, nrow) are left out."""
+    from segscan_gb300 import api
+    rng = np.random.default_rng(7)
+    nrow, nnz = 5000, 60000
+    rows = rng.integers(0, nrow, size=nnz).astype(np.int32)
+    if case == "sorted":
+        rows = np.sort(rows)
+    elif case == "skewed":
+        rows[: nnz // 2] = 17  # one row with half the entries (global-memory sort path)
+        rng.shuffle(rows)
+    elif case == "out_of_range":
+        rows[::97] = nrow + 3
+        rows[::89] = -1
+    elif case == "empty":
+        rows = rows[:0]
+    cols = rng.integers(0, 4000, size=rows.size).astype(np.int32)
+    vals = rng.standard_normal(rows.size).astype(np.float32)
+    A, perm = api.coo_to_csr(nrow, torch.from_numpy(rows).cuda(), torch.from_numpy(cols).cuda(), ncol=4000,
+                             values=torch.from_numpy(vals).cuda())
+    torch.cuda.synchronize()
+    valid = (rows >= 0) & (rows < nrow)
+    order = np.nonzero(valid)[0][np.argsort(rows[valid], kind="stable")].astype(np.int32)
+    indptr = np.concatenate([[0], np.cumsum(np.bincount(rows[valid], minlength=nrow))]).astype(np.int32)
+    m = int(valid.sum())
+    assert np.array_equal(A.indptr.cpu().numpy(), indptr)
+    assert np.array_equal(perm.cpu().numpy()[:m], order)
+    assert np.array_equal(A.indices.cpu().numpy()[:m], cols[order])
+    assert np.array_equal(A.values.cpu().numpy()[:m], vals[order])
