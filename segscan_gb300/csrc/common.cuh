@@ -64,25 +64,10 @@ __device__ __forceinline__ uint2 ld_u64(const void *p, uint64_t pol) {
                : "=r"(v.x), "=r"(v.y) : "l"(p), "l"(pol));
   return v;
 }
-#ifndef SS_LD128_HINT
-#define SS_LD128_HINT 0
-#endif
 __device__ __forceinline__ uint4 ld_u128(const void *p, uint64_t pol) {
   uint4 v;
-#if SS_LD128_HINT == 1
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
-#elif SS_LD128_HINT == 2
-  asm("ld.global.nc.L2::cache_hint.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
-#elif SS_LD128_HINT == 3
-  asm("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
-  (void)pol;
-#else
   asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
                : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
-#endif
   return v;
 }
 // Plain int loads for the index streams (A's columns, segment ids, indptr).
