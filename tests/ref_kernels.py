@@ -12,6 +12,7 @@ from pathlib import Path
 import torch
 
 CUBIN = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_kernels.cubin"
+SEG_CUBIN = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "ref_segment_kernels.cubin"
 
 
 def ceil_div(a, b):
@@ -87,3 +88,52 @@ class RefKernels:
         s = (stream or torch.cuda.current_stream()).cuda_stream
         self._check(self.cu.cuLaunchKernel(self.fn[strategy], grid[0], grid[1], grid[2], block[0], block[1], block[2],
                                            smem, ctypes.c_void_p(s), params, None), f"launch {strategy}")
+
+
+class RefSegmentKernels:
+    """Two of the reference's segment_coo kernels (new-cg/include/segscan/
+    segscan.cuh): segment_coo_sr<float, int, 4, 256, 4, 1, 1, 16> and the
+    segment_coo_sorted_sr<float, int, 2, 4, 8, 2, 16> that new-cg/src/main.cu
+    runs, with their launchers' geometry (segscan.cuh:817-829, 974-981).
+    Both add into dst, which the caller zeroes.  segscan_sr_kernel reads
+    index[] up to 15 entries past nnz (segscan.cuh:402, 459): `launch`
+    requires an index buffer padded by at least PAD entries."""
+
+    PAD = 32
+
+    def __init__(self):
+        torch.cuda.init()
+        torch.empty(1, device="cuda")
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        self.mod = ctypes.c_void_p()
+        RefKernels._check(self.cu.cuModuleLoad(ctypes.byref(self.mod), str(SEG_CUBIN).encode()), "cuModuleLoad")
+        self.fn = {}
+        for name in ("ref_seg_sr_n64", "ref_seg_sorted_sr"):
+            f = ctypes.c_void_p()
+            RefKernels._check(self.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name.encode()), name)
+            self.fn[name] = f
+
+    @staticmethod
+    def available() -> bool:
+        return SEG_CUBIN.exists()
+
+    def launch(self, which: str, src, index_padded, nnz: int, dst, stream=None):
+        N = int(src.shape[1])
+        assert index_padded.numel() >= nnz + self.PAD
+        if which == "sr":  # group 16, 256 threads, CoarsenFactor min(CEIL(N, 16), 4), block_factor 1/16
+            assert N == 64
+            grid, block, smem, fn = (int(nnz / 16), ceil_div(N, 16 * 4), 1), (256, 1, 1), 12 * 256, "ref_seg_sr_n64"
+        elif which == "sorted":  # CoarsenFactor 2, ThreadNz 4, DtileSize 8, DtileNum 2, BlockDimY 16
+            bx = min(2, ceil_div(N, 8 * 2)) * 8
+            by = min(16, ceil_div(nnz, 4))
+            grid, block, smem, fn = (ceil_div(N, bx * 2), ceil_div(nnz, by * 4), 1), (bx, by, 1), 0, "ref_seg_sorted_sr"
+            if grid[1] > 65535:
+                raise ValueError(f"segment_coo_sorted_sr's grid.y {grid[1]} exceeds 65535 (nnz {nnz})")
+        else:
+            raise ValueError(which)
+        vals = [ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(index_padded.data_ptr()), ctypes.c_int(nnz),
+                ctypes.c_int(N), ctypes.c_void_p(dst.data_ptr())]
+        params = (ctypes.c_void_p * len(vals))(*[ctypes.cast(ctypes.pointer(v), ctypes.c_void_p) for v in vals])
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        RefKernels._check(self.cu.cuLaunchKernel(self.fn[fn], grid[0], grid[1], grid[2], block[0], block[1], block[2],
+                                                 smem, ctypes.c_void_p(s), params, None), f"launch {fn}")

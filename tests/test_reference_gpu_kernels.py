@@ -95,3 +95,72 @@ def test_reference_kernel_timings(ref, capsys):
     with capsys.disabled():
         print("\nreference_kernels_sm103a " + json.dumps(rows))
     assert all(r["reference_ms"] > 0 for k_, r in rows.items() if k_ != "ours_tuned")
+
+
+# ---------------------------------------------------------------------------
+# segment_coo: the reference's segment_coo_sr and segment_coo_sorted_sr
+# ---------------------------------------------------------------------------
+from ref_kernels import RefSegmentKernels  # noqa: E402
+
+seg_available = pytest.mark.skipif(not RefSegmentKernels.available(),
+                                   reason="reference segment kernels not built (needs the reference checkout)")
+
+
+@pytest.fixture(scope="module")
+def ref_seg(cuda):
+    return RefSegmentKernels()
+
+
+def padded_index(index: np.ndarray) -> torch.Tensor:
+    """The index on the device with RefSegmentKernels.PAD copies of its last
+    id after it, so the reference kernel's reads past nnz stay in bounds."""
+    pad = np.full(RefSegmentKernels.PAD, index[-1], dtype=np.int32)
+    return torch.from_numpy(np.concatenate([index, pad])).cuda()
+
+
+@seg_available
+@pytest.mark.parametrize("which", ["sr", "sorted"])
+def test_reference_segment_kernels_match_ours(ref_seg, which):
+    import oracle_lib
+    csr = synth.powerlaw(30000, 30000, 2.1, 1, 3000, seed=24)
+    index = csr.coo_rows()
+    src = synth.dense(csr.nnz, 64, seed=25)
+    srcd = torch.from_numpy(src).cuda()
+    dst_ref = torch.zeros((csr.nrow, 64), device="cuda")
+    ref_seg.launch(which, srcd, padded_index(index), csr.nnz, dst_ref)
+    dst_ours = api.segment(srcd, torch.from_numpy(index).cuda(), csr.nrow, "sum")
+    torch.cuda.synchronize()
+    d64, dabs = oracle_lib.segment_coo_f64(src, index, csr.nrow, 0)
+    check_close(dst_ref.cpu().numpy(), d64, dabs, 1e-5, None, f"reference segment_coo {which} vs FP64")
+    check_close(dst_ours.cpu().numpy(), d64, dabs, 1e-5, None, "segscan_gb300 segment sum vs FP64")
+
+
+@seg_available
+def test_reference_segment_timings(ref_seg, capsys):
+    """segment sum over the power-law matrix's first 4,000,000 nonzeros
+    (segment_coo_sorted_sr's grid.y cannot hold the whole 4.63 M), N = 64,
+    dst zeroing included for the reference's atomic kernels."""
+    csr = synth.powerlaw(1_000_000, 1_000_000, 2.1, 1, 20000, seed=1)
+    nnz = 4_000_000
+    index = csr.coo_rows()[:nnz]
+    dst_len = int(index[-1]) + 1
+    srcd = torch.rand((nnz, 64), device="cuda")
+    idx_pad = padded_index(index)
+    idx = idx_pad[:nnz]
+    dst = torch.empty((dst_len, 64), device="cuda")
+    nbytes = synth.segment_bytes(nnz, 64, dst_len)
+    rows = {}
+    for which in ("sr", "sorted"):
+        def run():
+            dst.zero_()
+            ref_seg.launch(which, srcd, idx_pad, nnz, dst)
+        t = _ms(run)
+        rows[f"reference_{which}"] = {"ms": t, "GB/s": nbytes / t / 1e6}
+    ws_n = api.segment_workspace_size(nnz, 64, "sr")
+    t_ours = _ms(lambda: api.segment(srcd, idx, dst_len, "sum", "sr", out=dst))
+    best_ref = min(r["ms"] for r in rows.values())
+    rows["ours_sr"] = {"ms": t_ours, "GB/s": nbytes / t_ours / 1e6, "speedup_vs_best_reference": best_ref / t_ours,
+                       "workspace_bytes": ws_n}
+    with capsys.disabled():
+        print("\nreference_segment_kernels_sm103a " + json.dumps(rows))
+    assert all(r["ms"] > 0 for r in rows.values())
