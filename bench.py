@@ -275,6 +275,27 @@ def extra_precision(A, B, N, fp32_ms, dev):
         nb = synth.spmm_bytes(A, N, val_bytes=2, b_bytes=2, c_bytes=2 if cdt != torch.float32 else 4)
         out[name] = {"ms": ms, "GB/s": nb / ms / 1e6, "speedup_vs_fp32": fp32_ms / ms, "strategy": strategy,
                      "knobs": k.as_dict(), **_errors(Cd.float().cpu().numpy(), C64, absC)}
+    # the same at N = 128 (B and C twice as wide), against the FP32 time there
+    B128 = synth.dense(A.ncol, 128, seed=2)
+    C64, absC = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B128)
+    A32 = api.CsrMatrix.from_host(A, dev)
+    B32 = torch.from_numpy(B128).to(dev)
+    s32, k32 = autotune.best(A32, 128, B32)
+    C32 = torch.empty((A.nrow, 128), device=dev)
+    w32 = api.spmm_workspace_size(A32, 128, s32, k32)
+    ws32 = torch.empty(w32 + 256, dtype=torch.uint8, device=dev) if w32 else None
+    ms32 = _event_ms(lambda: api.spmm(A32, B32, s32, knobs=k32, out=C32, workspace=ws32), 20, stream)
+    del A32, B32, C32, ws32
+    Ad = api.CsrMatrix.from_host(A, dev, torch.bfloat16)
+    Bd = torch.from_numpy(B128).to(dev).to(torch.bfloat16)
+    strategy, k = autotune.best(Ad, 128, Bd)
+    Cd = torch.empty((A.nrow, 128), device=dev)
+    wsz = api.spmm_workspace_size(Ad, 128, strategy, k)
+    ws = torch.empty(wsz + 256, dtype=torch.uint8, device=dev) if wsz else None
+    ms = _event_ms(lambda: api.spmm(Ad, Bd, strategy, knobs=k, out=Cd, workspace=ws), 20, stream)
+    nb = synth.spmm_bytes(A, 128, val_bytes=2, b_bytes=2)
+    out["bf16_c_f32_n128"] = {"ms": ms, "GB/s": nb / ms / 1e6, "fp32_ms": ms32, "speedup_vs_fp32": ms32 / ms,
+                              "strategy": strategy, "knobs": k.as_dict(), **_errors(Cd.cpu().numpy(), C64, absC)}
     out["tolerance"] = "normwise <= 2e-2 vs FP64 on FP32 inputs"
     return out
 
@@ -593,6 +614,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic_from_profiles(kernel_file),
+                     "gather_upper_bound_bytes": A.nnz * N * 4 + A.nnz * 8 + (A.nrow + 1) * 4 + A.nrow * N * 4,
                      "kernel": (f"{strategy} SpMM step (walk with in-kernel carry assembly)" if strategy == "ebsr"
                                 else f"{strategy} SpMM step"),
                      "bytes_per_launch": nbytes},
