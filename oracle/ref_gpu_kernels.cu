@@ -1,5 +1,5 @@
-// The reference's own SpMM kernels (test-cg/include/spmm/spmm_cg.cuh),
-// compiled for sm_103a into a device-only cubin with plain extern "C"
+// The reference's own SpMM kernels (test-cg/include/spmm/spmm_cg.cuh) and
+// the dgSPARSE baseline kernels it includes (spmm.cuh), compiled for sm_103a into a device-only cubin with plain extern "C"
 // entry names, so bench.py can time them on the same GPU as this library
 // through the CUDA driver API.  MEASUREMENT INFRASTRUCTURE ONLY: built by
 // `make refgpu` from the reference sources where they lie (REF=<checkout>),
@@ -57,5 +57,26 @@ __global__ void ref_ebsr_n64(REF_ARGS_NNZ) {
 }
 __global__ void ref_rbsr_n64(REF_ARGS) {
   csrspmm_seqreduce_rowbalance_cg_kernel<float4, 32>(M, N, K, indptr, indices, data, B, C);
+}
+
+// The dgSPARSE baseline kernels the reference compares its static tuples
+// against (test-cg/include/spmm/spmm.cuh:17-637, README.md:212-260), with
+// the access widths their launchers pick for N a multiple of 4 (float4 for
+// ebpr/rbpr, spmm.cuh:172, 314) and the ebsr CoarsenFactor for N < 128 (1)
+// and 128 <= N < 512 (2) with ThreadNz 1 (spmm.cuh:525-529).
+__global__ void dg_ebpr_f4(REF_ARGS_NNZ) {
+  csrspmm_parreduce_nnzbalance_kernel<float4>(M, N, K, nnz, indptr, indices, data, B, C);
+}
+__global__ void dg_rbpr_f4(REF_ARGS) {
+  csrspmm_parreduce_rowbalance_kernel<float4>(M, N, K, indptr, indices, data, B, C);
+}
+__global__ void dg_ebsr_c1(REF_ARGS_NNZ) {
+  csrspmm_rowcaching_nnzbalance_kernel<1, 1>(M, N, K, nnz, indptr, indices, data, B, C);
+}
+__global__ void dg_ebsr_c2(REF_ARGS_NNZ) {
+  csrspmm_rowcaching_nnzbalance_kernel<2, 1>(M, N, K, nnz, indptr, indices, data, B, C);
+}
+__global__ void dg_rbsr(REF_ARGS) {
+  csrspmm_seqreduce_rowbalance_kernel(M, N, K, indptr, indices, data, B, C);
 }
 }

@@ -45,11 +45,16 @@ def features(A: api.CsrMatrix) -> dict:
             "frac_long": float((lengths > 32).sum()) / M}
 
 
+# bumped whenever the candidate list changes, so cached picks from an older
+# list are measured again
+CANDIDATES_REV = 2
+
+
 def signature(A: api.CsrMatrix, N: int, f: Optional[dict] = None) -> str:
     f = f or features(A)
     lg = lambda x: int(round(math.log2(max(1, x))))
     cvb = 0 if f["cv"] < 0.5 else 1 if f["cv"] < 2 else 2 if f["cv"] < 8 else 3
-    return f"M{lg(f['M'])}_nnz{lg(f['nnz'])}_mean{lg(f['mean'] + 1)}_max{lg(f['max'] + 1)}_cv{cvb}_N{N}_{A.dtype}"
+    return f"M{lg(f['M'])}_nnz{lg(f['nnz'])}_mean{lg(f['mean'] + 1)}_max{lg(f['max'] + 1)}_cv{cvb}_N{N}_{A.dtype}_c{CANDIDATES_REV}"
 
 
 def candidates(N: int, dtype: torch.dtype = torch.float32) -> list[tuple[str, dict]]:
@@ -69,8 +74,10 @@ def candidates(N: int, dtype: torch.dtype = torch.float32) -> list[tuple[str, di
                 for tpb in (128, 256, 512):
                     c.append(("ebsr", dict(group_factor=gf, coarsen_factor=vec, thread_nz=tnz, block_denom=1,
                                            thread_per_block=tpb)))
-    for cf, tf in ((4, 5), (4, 6), (2, 5)):
-        c.append(("rbsr", dict(coarsen_factor=cf, tile_factor=tf)))
+    # small blocks spread a small matrix's rows over more SMs
+    for cf, tf in ((4, 5), (4, 6), (2, 5), (2, 6)):
+        for tpb in (128, 256):
+            c.append(("rbsr", dict(coarsen_factor=cf, tile_factor=tf, thread_per_block=tpb)))
     return c
 
 
@@ -81,7 +88,8 @@ def heuristic(f: dict, N: int, dtype: torch.dtype = torch.float32) -> tuple[str,
     lanes_gf = max(0, min(5, int(math.log2(max(1, N // vec)))))
     if f["cv"] > 1.0 or f["max"] > 256:
         return "ebsr", dict(group_factor=lanes_gf, coarsen_factor=vec, thread_nz=8, block_denom=1)
-    return "rbsr", dict(coarsen_factor=4, tile_factor=max(0, min(7, int(math.log2(max(1, N))))))
+    return "rbsr", dict(coarsen_factor=4, tile_factor=max(0, min(7, int(math.log2(max(1, N))))),
+                        thread_per_block=128)
 
 
 def _load_disk() -> dict:

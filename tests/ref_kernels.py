@@ -90,6 +90,58 @@ class RefKernels:
                                            smem, ctypes.c_void_p(s), params, None), f"launch {strategy}")
 
 
+class DgKernels:
+    """The dgSPARSE baseline kernels (test-cg/include/spmm/spmm.cuh:17-637)
+    from the same cubin, with their launchers' geometry (spmm.cuh:167-200,
+    310-343, 522-590, 621-637; RefThreadPerBlock 256, check.cuh:13), for N a
+    multiple of 4 up to 256: the widths the launchers would pick there
+    (float4 for ebpr/rbpr, ebsr CoarsenFactor 1 below N = 128 and 2 from
+    128), and rbsr's one thread per (row, column) stays inside N."""
+
+    TPB = 256
+
+    def __init__(self, ref: RefKernels):
+        self.cu, self.mod = ref.cu, ref.mod
+        self.fn = {}
+        for name in ("dg_ebpr_f4", "dg_rbpr_f4", "dg_ebsr_c1", "dg_ebsr_c2", "dg_rbsr"):
+            f = ctypes.c_void_p()
+            RefKernels._check(self.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name.encode()), name)
+            self.fn[name] = f
+
+    def geometry(self, strategy: str, M: int, N: int):
+        """(kernel, grid, block, smem) as the dgSPARSE launcher computes them."""
+        assert N % 4 == 0 and 0 < N <= 256, N
+        if strategy in ("ebpr", "rbpr"):
+            cf = 4
+            ndim_tb = ceil_div(N, 32)
+            ndim_warp = min(N, 32) // cf
+            warp_per_tb = ceil_div(self.TPB // 32, ndim_warp)
+            return (f"dg_{strategy}_f4", (ceil_div(M, warp_per_tb), ndim_tb, 1), (ndim_warp * 32, warp_per_tb, 1), 0)
+        if strategy == "ebsr":
+            cf = 2 if N >= 128 else 1
+            return (f"dg_ebsr_c{cf}", (ceil_div(M, self.TPB // 32), ceil_div(N, 32 * cf), 1), (self.TPB, 1, 1),
+                    12 * self.TPB)
+        if strategy == "rbsr":
+            nthr = min(N, self.TPB)
+            mthr = ceil_div(self.TPB, nthr)
+            return "dg_rbsr", (ceil_div(M, mthr), ceil_div(N, self.TPB), 1), (nthr, mthr, 1), 0
+        raise ValueError(strategy)
+
+    def launch(self, strategy: str, M: int, K: int, nnz: int, indptr, indices, data, B, C, stream=None):
+        """One launch; C must be zeroed first for all but rbsr."""
+        N = int(B.shape[1])
+        fn, grid, block, smem = self.geometry(strategy, M, N)
+        ints = [ctypes.c_int(M), ctypes.c_int(N), ctypes.c_int(K)]
+        if strategy in ("ebpr", "ebsr"):
+            ints.append(ctypes.c_int(nnz))
+        ptrs = [ctypes.c_void_p(t.data_ptr()) for t in (indptr, indices, data, B, C)]
+        vals = ints + ptrs
+        params = (ctypes.c_void_p * len(vals))(*[ctypes.cast(ctypes.pointer(v), ctypes.c_void_p) for v in vals])
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        RefKernels._check(self.cu.cuLaunchKernel(self.fn[fn], grid[0], grid[1], grid[2], block[0], block[1], block[2],
+                                                 smem, ctypes.c_void_p(s), params, None), f"launch {fn}")
+
+
 class RefSegmentKernels:
     """Two of the reference's segment_coo kernels (new-cg/include/segscan/
     segscan.cuh): segment_coo_sr<float, int, 4, 256, 4, 1, 1, 16> and the

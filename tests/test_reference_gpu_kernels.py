@@ -10,6 +10,7 @@ result.  The timing test prints the reference kernels' times beside this
 library's for the power-law 1e6 x 1e6 workload (C zeroing included for the
 reference's atomic strategies, as its driver does at test.cu:58-82)."""
 import json
+import os
 
 import numpy as np
 import pytest
@@ -164,3 +165,104 @@ def test_reference_segment_timings(ref_seg, capsys):
     with capsys.disabled():
         print("\nreference_segment_kernels_sm103a " + json.dumps(rows))
     assert all(r["ms"] > 0 for r in rows.values())
+
+
+# ---------------------------------------------------------------------------
+# dgSPARSE baseline kernels (spmm.cuh) and the README's "static vs dgSPARSE"
+# ---------------------------------------------------------------------------
+from ref_kernels import DgKernels  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def dg(ref):
+    return DgKernels(ref)
+
+
+@pytest.mark.parametrize("strategy,N", [("ebpr", 64), ("rbpr", 64), ("ebsr", 64), ("rbsr", 64), ("ebsr", 128),
+                                        ("ebpr", 128), ("rbpr", 20)])
+def test_dgsparse_kernels_match_fp64(dg, strategy, N):
+    A = integer_valued(synth.powerlaw(30000, 30000, 2.1, 1, 3000, seed=26), 27)
+    B = synth.dense(A.ncol, N, seed=28)
+    Ad = dev_csr(A)
+    Bd = torch.from_numpy(B).cuda()
+    C = torch.zeros((A.nrow, N), device="cuda")
+    dg.launch(strategy, A.nrow, A.ncol, A.nnz, Ad.indptr, Ad.indices, Ad.values, Bd, C)
+    torch.cuda.synchronize()
+    C64, absC = oracle64(A, B)
+    check_close(C.cpu().numpy(), C64, absC, 1e-5, None, f"dgSPARSE {strategy} N={N} vs FP64")
+
+
+# README.md:212-260 quotes, per strategy, dgSPARSE time / best static tuple
+# time (geomean over SuiteSparse).  Seeded synthetic matrices of the
+# configurations' shapes and a few more row-length distributions stand in for
+# the SuiteSparse set, which is not available.
+SWEEP_DATASETS = ["poisson:4096:16:0", "poisson:200000:16:0", "banded:120000:20:500:1", "banded:400000:48:2000:1",
+                  "powerlaw:1000000:2.1:20000:1", "powerlaw:300000:1.8:50000:5", "powerlaw:600000:2.6:2000:6"]
+REF_TUPLES = {"ebpr": dict(group_factor=5, thread_per_block=256, tile_factor=5, block_numer=1, block_denom=16),
+              "rbpr": dict(group_factor=3, thread_per_block=256, tile_factor=3, block_numer=1, block_denom=2),
+              "ebsr": dict(group_factor=4, thread_per_block=256, coarsen_factor=4, thread_nz=1, block_numer=1,
+                           block_denom=16),
+              "rbsr": dict(coarsen_factor=4, thread_per_block=256, tile_factor=5, block_numer=1, block_denom=1)}
+
+
+def test_static_vs_dgsparse_sweep(ref, dg, capsys, tmp_path):
+    from segscan_gb300 import ratios, sweep
+    from segscan_gb300.ratios import Row
+
+    same = {s: sweep.label(s, api.make_knobs(s, N, **kw)) for s, kw in REF_TUPLES.items()}
+    swept = {sweep.label(s, k) for s, k in sweep.library_actions(N)}
+
+    def extra(spec, Ah, A, B, timer):
+        C = torch.empty((Ah.nrow, N), device="cuda")
+        rows = []
+        for s, kw in REF_TUPLES.items():  # this library at the reference's tuples, where the sweep lacks them
+            if same[s] not in swept:
+                k = api.make_knobs(s, N, **kw)
+                n = api.spmm_workspace_size(A, N, s, k)
+                ws = torch.empty(n + 256, dtype=torch.uint8, device="cuda") if n else None
+                rows.append(Row(spec, N, same[s], "library",
+                                timer(lambda: api.spmm(A, B, s, knobs=k, out=C, workspace=ws))))
+        for s in ("ebpr", "rbpr", "ebsr", "rbsr"):
+            zero = s != "rbsr"
+
+            def run_ref():
+                if zero:
+                    C.zero_()
+                ref.launch(s, Ah.nrow, Ah.ncol, Ah.nnz, A.indptr, A.indices, A.values, B, C)
+
+            def run_dg():
+                if zero:
+                    C.zero_()
+                dg.launch(s, Ah.nrow, Ah.ncol, Ah.nnz, A.indptr, A.indices, A.values, B, C)
+            rows.append(Row(spec, N, f"reference_{s}", "external", timer(run_ref)))
+            rows.append(Row(spec, N, f"dgsparse_{s}", "external", timer(run_dg)))
+        return rows
+
+    rows = sweep.run(SWEEP_DATASETS, N, iters=11, extra=extra)
+    ratios.write_csv(os.environ.get("SEGSCAN_SWEEP_CSV") or tmp_path / "sweep.csv", rows)
+    out = {"datasets": SWEEP_DATASETS, "N": N, "timing": "median of 11 CUDA-event launches, L2 flushed before each"}
+    for s in ("ebpr", "rbpr", "ebsr", "rbsr"):
+        out[s] = {"reference_static_vs_dgsparse": ratios.compare(rows, f"dgsparse_{s}", f"reference_{s}"),
+                  "ours_same_tuple_vs_dgsparse": ratios.compare(rows, f"dgsparse_{s}", same[s]),
+                  "ours_same_tuple_vs_reference": ratios.compare(rows, f"reference_{s}", same[s]),
+                  "same_tuple": same[s]}
+    lib_actions = [r.action for r in rows if r.kind == "library" and r.dataset == SWEEP_DATASETS[0]]
+    out["tuning"] = ratios.tuning(rows, sweep.label("ebsr", api.default_knobs("ebsr", N)), lib_actions)
+    st = ratios.static_ranking(rows, lib_actions)
+    out["best_static"] = st["best_static"]
+    best_lib, best_ref, best_act = {}, {}, {}
+    table = ratios.pivot(rows)
+    for key, t in table.items():
+        best_act[key] = min((a for a in lib_actions if a in t), key=lambda a: t[a])
+        best_lib[key] = t[best_act[key]]
+        best_ref[key] = min(t[f"reference_{s}"] for s in ("ebpr", "rbpr", "ebsr", "rbsr"))
+    r = [best_ref[k] / best_lib[k] for k in table]
+    out["best_ours_vs_best_reference_kernel"] = ratios.stats(r)
+    out["per_dataset_us"] = {k[0]: {"best_ours": best_lib[k], "best_ours_action": best_act[k],
+                                    "best_reference": best_ref[k],
+                                    "cusparse": table[k].get("cusparse"),
+                                    **{f"dgsparse_{s}": table[k][f"dgsparse_{s}"] for s in REF_TUPLES}}
+                             for k in table}
+    with capsys.disabled():
+        print("\nstatic_vs_dgsparse_sm103a " + json.dumps(out))
+    assert len(table) == len(SWEEP_DATASETS)
