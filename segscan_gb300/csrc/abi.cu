@@ -300,6 +300,12 @@ static ss_status make_spmm_call(int strategy, const ss_csr *A, int N, const void
   return SS_OK;
 }
 
+// Fewer than half as many nonzeros as output rows: at least half the rows
+// are empty, and the element-balanced kernels would zero their runs one
+// team per run.  Zeroing the output with a memset and accumulating is
+// cheaper there; the sums are the same (0 + x = x).
+static bool hypersparse(long long nnz, long long rows) { return 2 * nnz < rows; }
+
 // Vector accesses need the B/C row starts aligned to V elements.
 static ss_status check_vec_alignment(const void *B, const void *C, int es, int cs, int V) {
   if (((uintptr_t)B % (size_t)(es * V)) || ((uintptr_t)C % (size_t)(cs * V)))
@@ -422,6 +428,13 @@ ss_status ss_spmm(int strategy, const ss_csr *A, int N, const void *B, void *C, 
     const size_t need = eb_workspace_bytes(eg, N);
     if (ws_bytes < need || (need > 0 && (!ws || ((uintptr_t)ws % 256))))
       return fail(SS_ERR_WORKSPACE, "workspace needs %zu bytes (256-byte aligned), got %zu", need, ws_bytes);
+    if (!accumulate && hypersparse(c.nnz, c.M)) {
+      // at least half the rows are empty: zero C at copy bandwidth and add
+      // into it, instead of chunks writing long runs of empty rows alone
+      cudaError_t e = cudaMemsetAsync(C, 0, (size_t)c.M * c.N * dtype_size(c.c_dtype), s);
+      if (e != cudaSuccess) return cuda_fail(e, "zero C");
+      c.accumulate = 1;
+    }
     return strategy == SS_EBSR ? launch_ebsr(c, eg, ws, s) : launch_ebpr(c, eg, ws, s);
   }
   return strategy == SS_RBSR ? launch_rbsr(c, rg, s) : launch_rbpr(c, rg, s);
@@ -509,6 +522,11 @@ ss_status ss_segment_coo(int seg_strategy, const void *src, int src_dtype, const
   SegCall c;
   c.nnz = nnz; c.N = N; c.dst_len = dst_len; c.src = src; c.src_dtype = src_dtype; c.index = index;
   c.dst = dst; c.reduce = reduce; c.accumulate = accumulate;
+  if (!accumulate && reduce == SS_SUM && hypersparse(nnz, dst_len)) {
+    cudaError_t e = cudaMemsetAsync(dst, 0, (size_t)dst_len * N * sizeof(float), s);
+    if (e != cudaSuccess) return cuda_fail(e, "zero dst");
+    c.accumulate = 1;
+  }
   c.kahan_threshold = knobs->kahan_threshold > 0 ? knobs->kahan_threshold : 1024;
   return seg_strategy == SS_SEG_SR ? launch_seg_sr(c, g, ws, s) : launch_seg_pr(c, g, ws, s);
 }

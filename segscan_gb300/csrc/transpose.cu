@@ -5,7 +5,8 @@
 // sort by column: entries of one column keep A's CSR order.  The device
 // version gives the same result bit for bit:
 //   1. column histogram (atomics)            -> counts
-//   2. exclusive scan of counts (3 kernels)  -> t_indptr
+//   2. exclusive scan of counts (3 kernels; 5 when K > 4096^2, the tile
+//      sums then scanned in two levels)      -> t_indptr
 //   3. scatter nonzero ids by column (atomic cursors; order inside a column
 //      is arbitrary here)                    -> perm
 //   4. sort each column's ids ascending      -> the stable order
@@ -26,18 +27,25 @@ constexpr int SMEM_SORT_MAX = 16384;
 struct TransposeWs {
   int32_t *counts;    // [K + 1]
   int32_t *cursor;    // [K]
-  int32_t *bsum;      // [SCAN_TILE]
+  int32_t *bsum;      // [tiles]: per-tile sums, then (one level) their exclusive scan
+  int32_t *bsum_scan; // [tiles]: the exclusive scan of bsum (two levels)
+  int32_t *bsum2;     // [SCAN_TILE]: sums of bsum's tiles (two levels)
   int32_t *rowid;     // [nnz]
   int32_t *work;      // [1 + K]: count, then column ids with > 32 entries
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+static long long scan_tiles(long long n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+
 static size_t transpose_ws_bytes(int K, int nnz, TransposeWs *w, void *base) {
+  const size_t tiles = (size_t)std::max(1LL, scan_tiles(K));
   size_t o = 0;
   const size_t counts = o; o += align256((size_t)(K + 1) * 4);
   const size_t cursor = o; o += align256((size_t)K * 4);
-  const size_t bsum = o; o += align256((size_t)SCAN_TILE * 4);
+  const size_t bsum = o; o += align256(tiles * 4);
+  const size_t bsum_scan = o; o += align256(tiles * 4);
+  const size_t bsum2 = o; o += align256((size_t)SCAN_TILE * 4);
   const size_t rowid = o; o += align256((size_t)nnz * 4);
   const size_t work = o; o += align256((size_t)(K + 1) * 4);
   if (w) {
@@ -45,6 +53,8 @@ static size_t transpose_ws_bytes(int K, int nnz, TransposeWs *w, void *base) {
     w->counts = (int32_t *)(b + counts);
     w->cursor = (int32_t *)(b + cursor);
     w->bsum = (int32_t *)(b + bsum);
+    w->bsum_scan = (int32_t *)(b + bsum_scan);
+    w->bsum2 = (int32_t *)(b + bsum2);
     w->rowid = (int32_t *)(b + rowid);
     w->work = (int32_t *)(b + work);
   }
@@ -259,7 +269,7 @@ __global__ void gather_rows_kernel(const int32_t *__restrict__ perm, const int32
 // start, perm the positions grouped by key, ascending within a key.
 static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out_indptr, int32_t *perm,
                                const TransposeWs &w, cudaStream_t s) {
-  const long long tiles = ((long long)K + SCAN_TILE - 1) / SCAN_TILE;
+  const long long tiles = scan_tiles(K);
   cudaError_t e = cudaMemsetAsync(w.counts, 0, (size_t)(K + 1) * 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.work, 0, 4, s);
   if (e != cudaSuccess) return cuda_fail(e, "counting sort clear");
@@ -269,8 +279,18 @@ static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out
   }
   if (nnz > 0) hist_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(keys, nnz, K, w.counts);
   scan_tile_kernel<<<(int)tiles, 1024, 0, s>>>(w.counts, K, out_indptr, w.bsum);
-  scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, (int)tiles, out_indptr + K);
-  scan_add_kernel<<<grid_for(K, 256), 256, 0, s>>>(out_indptr, K, w.bsum);
+  if (tiles <= SCAN_TILE) {
+    scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum, (int)tiles, out_indptr + K);
+    scan_add_kernel<<<grid_for(K, 256), 256, 0, s>>>(out_indptr, K, w.bsum);
+  } else {
+    // the tile sums are themselves more than one tile: scan them the same
+    // way (at most 4096 second-level tiles for any int32 K)
+    const long long tiles2 = scan_tiles(tiles);
+    scan_tile_kernel<<<(int)tiles2, 1024, 0, s>>>(w.bsum, (int)tiles, w.bsum_scan, w.bsum2);
+    scan_bsum_kernel<<<1, 1024, 0, s>>>(w.bsum2, (int)tiles2, out_indptr + K);
+    scan_add_kernel<<<grid_for(tiles, 256), 256, 0, s>>>(w.bsum_scan, (int)tiles, w.bsum2);
+    scan_add_kernel<<<grid_for(K, 256), 256, 0, s>>>(out_indptr, K, w.bsum_scan);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "counting sort scan");
   if (nnz == 0) return SS_OK;
@@ -304,8 +324,6 @@ ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indice
   const int M = A->nrow, K = A->ncol, nnz = A->nnz;
   if (!t_indptr || (nnz > 0 && (!t_indices || !perm || !A->indices || !A->indptr)))
     return fail(SS_ERR_INVALID_ARG, "null pointer");
-  const long long tiles = ((long long)K + SCAN_TILE - 1) / SCAN_TILE;
-  if (tiles > SCAN_TILE) return fail(SS_ERR_CAPACITY, "ncol %d above the scan capacity %d", K, SCAN_TILE * SCAN_TILE);
   const size_t need = transpose_ws_bytes(K, nnz, nullptr, nullptr);
   if (ws_bytes < need || !ws || ((uintptr_t)ws % 256))
     return fail(SS_ERR_WORKSPACE, "workspace needs %zu bytes (256-byte aligned), got %zu", need, ws_bytes);
@@ -331,8 +349,6 @@ ss_status ss_coo_to_csr(int nrow, int nnz, const int32_t *rows, const int32_t *c
   ss::NvtxRange nvtx_range("ss_coo_to_csr");
   if (nrow < 0 || nnz < 0 || !indptr || (nnz > 0 && (!rows || !cols || !out_cols || !perm)))
     return fail(SS_ERR_INVALID_ARG, "bad arguments");
-  const long long tiles = ((long long)nrow + SCAN_TILE - 1) / SCAN_TILE;
-  if (tiles > SCAN_TILE) return fail(SS_ERR_CAPACITY, "nrow %d above the scan capacity %d", nrow, SCAN_TILE * SCAN_TILE);
   const size_t need = transpose_ws_bytes(nrow, nnz, nullptr, nullptr);
   if (ws_bytes < need || !ws || ((uintptr_t)ws % 256))
     return fail(SS_ERR_WORKSPACE, "workspace needs %zu bytes (256-byte aligned), got %zu", need, ws_bytes);

@@ -20,7 +20,7 @@ comparison kernel that is not cuSPARSE); it is written and read as CSV.
 Times come from `segscan_gb300.sweep` (CUDA events) or from an ncu launch
 list (`from_ncu_csv`), which is what the reference's tables hold.
 
-    python -m segscan_gb300.ratios table.csv --default "ebsr:default"
+    python -m segscan_gb300.ratios table.csv --default "ebsr(4,256,4,2,1,16)"
 """
 from __future__ import annotations
 
