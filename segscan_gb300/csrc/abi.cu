@@ -487,7 +487,7 @@ ss_status ss_segment_coo_workspace_size(int seg_strategy, int nnz, int N, const 
   EbGeom g;
   ss_status st = seg_geometry(seg_strategy, nnz, N, SS_F32, *knobs, g);
   if (st) return st;
-  *bytes = eb_workspace_bytes(g, N);
+  *bytes = seg_strategy == SS_SEG_SR ? seg_sr_workspace_bytes(g, N) : eb_workspace_bytes(g, N);
   return SS_OK;
 }
 
@@ -516,7 +516,7 @@ ss_status ss_segment_coo(int seg_strategy, const void *src, int src_dtype, const
     cudaError_t e = cudaMemsetAsync(dst, 0, (size_t)dst_len * N * sizeof(float), s);
     return e == cudaSuccess ? SS_OK : cuda_fail(e, "zero dst");
   }
-  const size_t need = eb_workspace_bytes(g, N);
+  const size_t need = seg_strategy == SS_SEG_SR ? seg_sr_workspace_bytes(g, N) : eb_workspace_bytes(g, N);
   if (ws_bytes < need || !ws || ((uintptr_t)ws % 256))
     return fail(SS_ERR_WORKSPACE, "workspace needs %zu bytes (256-byte aligned), got %zu", need, ws_bytes);
   SegCall c;

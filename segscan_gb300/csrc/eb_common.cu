@@ -22,6 +22,10 @@ size_t eb_workspace_bytes(const EbGeom &g, int N) {
   return carry_rows_bytes(g.num_chunks, g.cs.tiles) + 2 * (size_t)g.num_chunks * (size_t)N * sizeof(float);
 }
 
+size_t seg_sr_workspace_bytes(const EbGeom &g, int N) {
+  return eb_workspace_bytes(g, N) + (((size_t)2 * g.num_chunks * sizeof(int32_t) + 255) & ~(size_t)255);
+}
+
 CarryView carry_view(void *ws, int num_chunks, int N, int tiles) {
   CarryView cv;
   size_t rows = carry_rows_bytes(num_chunks, tiles);
@@ -51,6 +55,7 @@ EbArgs eb_base_args(const EbGeom &g, void *ws, int N) {
   a.carry_vals = cv.vals;
   a.tail_vals = cv.tails;
   a.carry_cnt = cv.rows;
+  a.seg_cnt = nullptr;
   return a;
 }
 

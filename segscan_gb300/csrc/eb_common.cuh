@@ -8,8 +8,9 @@
 // the last row (continues into the next chunk).  Their FP32 partials go to
 // the chunk's head and tail slots, and each straddling row is assembled
 // once as owner tail + following heads (by the last of its chunks to finish,
-// carry_arrive, in the ebsr and batched walks; by the fix-up kernel,
-// fixup_chunk, after the ebpr and segment kernels) and stored once, so a
+// carry_arrive / seg_carry_arrive, in the ebsr, segment SR and batched
+// walks; by the fix-up kernel, fixup_chunk, after the ebpr and segment PR
+// kernels) and stored once, so a
 // 16-bit output is rounded once.  Empty rows (empty
 // segments) are written as zero by the chunk holding the next nonzero, so in
 // overwrite mode every output row is written exactly once, no zero fill and
@@ -45,6 +46,8 @@ struct EbArgs {
   float *carry_vals;    // [num_chunks * N] head-row partials
   float *tail_vals;     // [num_chunks * N] partial of a last row that continues
   int *carry_cnt;       // [num_chunks * column tiles] arrivals per straddling row (zeroed per launch)
+  int *seg_cnt;         // segment SR walk: [2 * num_chunks] elements of the owner's tail segment
+                        // (k) and of the head segment (num_chunks + k) in chunk k, for means
 };
 
 struct ChunkInfo {
@@ -212,6 +215,113 @@ __device__ __forceinline__ void carry_arrive(const EbArgs &a, int r, int lane, i
       for (int i = 0; i < V; i++) acc[i] += prev[i];
     }
     store_vec<TC, V>(dst, acc, pol);
+  }
+}
+
+// ---------------------------------------------------------------------
+// In-kernel carry assembly of the segment SR walk.  A segment has no
+// row pointer, so the chunks it spans are found from chunk boundaries: a
+// chunk j > o holds part of segment r iff index[j * chunk] == r, and the
+// owner o is the last chunk before the participant whose first id is
+// smaller than r (or 0).  Each lane of a group probes one boundary; the
+// first round's probes are loaded when the chunk starts, so their latency
+// overlaps the walk.
+// ---------------------------------------------------------------------
+__device__ __forceinline__ unsigned group_ballot(unsigned mask, bool pred, int G) {
+  const unsigned bits = G >= 32 ? 0xffffffffu : ((1u << G) - 1u);
+  const unsigned shift = (threadIdx.x & 31u) & ~(unsigned)(G - 1);
+  return (__ballot_sync(mask, pred) >> shift) & bits;
+}
+
+// index[(chunk - 1 - lane) * a.chunk], INT_MIN before the array
+__device__ __forceinline__ int seg_probe_back(const EbArgs &a, int chunk, int lane) {
+  const long long j = (long long)chunk - 1 - lane;
+  return j >= 0 ? __ldg(a.index + j * a.chunk) : INT_MIN;
+}
+// index[(chunk + 1 + lane) * a.chunk], INT_MAX past the array
+__device__ __forceinline__ int seg_probe_fwd(const EbArgs &a, int chunk, int lane) {
+  const long long e = ((long long)chunk + 1 + lane) * a.chunk;
+  return e < a.nnz ? __ldg(a.index + e) : INT_MAX;
+}
+
+// Owner chunk of segment r, which continues into `chunk` from before it;
+// `back` is this lane's seg_probe_back(chunk).
+__device__ __forceinline__ int seg_owner(const EbArgs &a, int r, int chunk, int back, int lane, int G,
+                                         unsigned mask) {
+  int base = chunk - 1;  // lane i holds the first id of chunk base - i
+  int v = back;
+  while (true) {
+    const unsigned m = group_ballot(mask, v < r, G);
+    if (m) return max(base - (__ffs(m) - 1), 0);  // a probe before the array: r starts at 0
+    base -= G;  // every probe was r: r started before all of them (base >= G here)
+    v = seg_probe_back(a, base + 1, lane);
+  }
+}
+
+// Last chunk holding part of segment r, which `chunk` holds and which
+// continues past it; `fwd` is this lane's seg_probe_fwd(chunk).
+__device__ __forceinline__ int seg_last(const EbArgs &a, int r, int chunk, int fwd, int lane, int G,
+                                        unsigned mask) {
+  int base = chunk + 1;  // lane i holds the first id of chunk base + i
+  int v = fwd;
+  while (true) {
+    const unsigned m = group_ballot(mask, v != r, G);
+    if (m) return base + (__ffs(m) - 1) - 1;
+    base += G;
+    v = seg_probe_fwd(a, base - 1, lane);
+  }
+}
+
+// carry_arrive for segment r spanning chunks o..l: the last participant
+// combines tail(o) and heads(o+1..l) in chunk order (Kahan sum, or max),
+// divides a mean by the segment's length (owner's tail count + full middle
+// chunks + the last chunk's head count) and stores dst once; the same
+// arithmetic in the same order as fixup_chunk.
+template <int V, int NV>
+__device__ __forceinline__ void seg_carry_arrive(const EbArgs &a, int r, int o, int l, int lane, int G,
+                                              unsigned mask, int col0, const bool (&act)[NV], uint64_t pol) {
+  if ((unsigned)r >= (unsigned)a.M) return;  // every participant sees the same r: none counts
+  int *cnt = a.carry_cnt + (size_t)o * gridDim.y + blockIdx.y;
+  __threadfence();  // this lane's slot and count stores are visible before the count moves
+  __syncwarp(mask);
+  int last = 0;
+  if (lane == 0) last = atomicAdd(cnt, 1) == l - o;
+  last = __shfl_sync(mask, last, 0, G);
+  if (!last) return;
+  __threadfence();  // every other participant's stores are visible now
+  const bool is_max = a.reduce == SS_MAX;
+  float count = 1.f;
+  if (a.reduce == SS_MEAN)
+    count = (float)(__ldcg(a.seg_cnt + o) + (l - o - 1) * a.chunk + __ldcg(a.seg_cnt + a.num_chunks + l));
+  float *C = (float *)a.C;
+  #pragma unroll
+  for (int j = 0; j < NV; j++) {
+    if (!act[j]) continue;
+    const int64_t col = col0 + j * V;
+    float acc[V], comp[V], x[V];
+    load_slot<V>(a.tail_vals + (int64_t)o * a.N + col, acc);
+    #pragma unroll
+    for (int i = 0; i < V; i++) comp[i] = 0.f;
+    for (int k = o + 1; k <= l; k++) {
+      load_slot<V>(a.carry_vals + (int64_t)k * a.N + col, x);
+      #pragma unroll
+      for (int i = 0; i < V; i++) {
+        if (is_max) acc[i] = fmaxf(acc[i], x[i]);
+        else kahan_add(acc[i], comp[i], x[i]);
+      }
+    }
+    float *dst = C + (int64_t)r * a.N + col;
+    if (a.accumulate) {
+      float prev[V];
+      load_out<float, V>(dst, prev);
+      #pragma unroll
+      for (int i = 0; i < V; i++) acc[i] += prev[i];
+    }
+    if (a.reduce == SS_MEAN) {
+      #pragma unroll
+      for (int i = 0; i < V; i++) acc[i] = acc[i] / count;
+    }
+    store_vec<float, V>(dst, acc, pol);
   }
 }
 

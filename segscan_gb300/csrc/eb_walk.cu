@@ -87,14 +87,18 @@ ss_status launch_seg_sr(const SegCall &c, const EbGeom &g, void *ws, cudaStream_
   a.accumulate = c.accumulate; a.reduce = c.reduce; a.kahan = c.kahan_threshold;
   a.use_tma = aligned16(c.index) && (g.chunk % 8) == 0;
   a.err = walk_error_ptr();
+  a.seg_cnt = (int *)((char *)ws + eb_workspace_bytes(g, c.N));
   void *fn = nullptr;
   if (c.src_dtype == SS_F32) fn = sr_kernel_f32(g.cs.V, g.cs.NV, true);
   else if (c.src_dtype == SS_BF16) fn = sr_kernel_bf16(g.cs.V, g.cs.NV, true, true);
   else fn = sr_kernel_f16(g.cs.V, g.cs.NV, true, true);
-  ss_status st = run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, 0), s, "segment_coo sr launch");
-  if (st != SS_OK) return st;
-  return launch_fixup(carry_view(ws, g.num_chunks, c.N, g.cs.tiles), g.num_chunks, c.N, c.dst_len, c.dst, SS_F32, c.reduce,
-                      c.accumulate, c.index, c.nnz, s);
+  // straddling segments are assembled inside the walk (seg_carry_arrive):
+  // arrival counts need zeroing, no fix-up launch follows
+  if (g.num_chunks > 0) {
+    cudaError_t e = cudaMemsetAsync(a.carry_cnt, 0, carry_rows_bytes(g.num_chunks, g.cs.tiles), s);
+    if (e != cudaSuccess) return cuda_fail(e, "segment carry counts");
+  }
+  return run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, 0), s, "segment_coo sr launch");
 }
 
 }  // namespace ss

@@ -447,12 +447,16 @@ __device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lan
   ci.r_last = ci.r_first;
   ci.prev_row = ci.cs > 0 ? __ldg(a.index + ci.cs - 1) : -1;
   ci.has_head = ci.cs > 0 && ci.prev_row == ci.r_first;
-  if (blockIdx.y == 0 && lane == 0) a.carry_rows[chunk] = ci.has_head ? ci.r_first : -1;
+  const int head = ci.has_head ? ci.r_first : -1;
+  // chunk-boundary probes for the carry assembly at the end, in flight now
+  const int probe_back = head >= 0 ? seg_probe_back(a, chunk, lane) : INT_MIN;
+  const int probe_fwd = seg_probe_fwd(a, chunk, lane);
   if (!a.accumulate && !ci.has_head)
     zero_rows<float, V, NV>(a, ci.prev_row + 1, ci.r_first - 1, col0, act, strm);
 
   int cur = ci.r_first;
   int cnt = 0;
+  int head_n = 0;  // elements of the head segment in this chunk
   float acc[NV][V], comp[NV][V];
   #pragma unroll
   for (int j = 0; j < NV; j++)
@@ -486,6 +490,7 @@ __device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lan
         const int r = sidx[q + u];
         if (r != cur) {
           flush_row<float, V, NV>(a, ci, chunk, cur, acc, cnt, true, col0, act, strm);
+          if (cur == head) head_n = cnt;
           if (!a.accumulate) zero_rows<float, V, NV>(a, cur + 1, r - 1, col0, act, strm);
           cur = r;
           cnt = 0;
@@ -510,7 +515,25 @@ __device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lan
   }
   const bool complete = ci.ce >= a.nnz || __ldg(a.index + ci.ce) != cur;
   flush_row<float, V, NV>(a, ci, chunk, cur, acc, cnt, complete, col0, act, strm);
+  if (cur == head) head_n = cnt;
   if (!a.accumulate && ci.ce >= a.nnz) zero_rows<float, V, NV>(a, cur + 1, a.M - 1, col0, act, strm);
+  // straddling segments: count this chunk in (head, then a tail that
+  // continues), the last participant of each stores it
+  const bool tail = !complete && cur != head;
+  const bool mean = a.reduce == SS_MEAN;
+  if (head >= 0 && (unsigned)head < (unsigned)a.M) {
+    const int o = seg_owner(a, head, chunk, probe_back, lane, G, mask);
+    const int l = seg_last(a, head, chunk, probe_fwd, lane, G, mask);
+    // every column tile writes the count (the same value): the last arriver
+    // of any tile may read it
+    if (mean && l == chunk && lane == 0) a.seg_cnt[a.num_chunks + chunk] = head_n;
+    seg_carry_arrive<V, NV>(a, head, o, l, lane, G, mask, col0, act, strm);
+  }
+  if (tail && (unsigned)cur < (unsigned)a.M) {
+    const int l = seg_last(a, cur, chunk, probe_fwd, lane, G, mask);
+    if (mean && lane == 0) a.seg_cnt[chunk] = cnt;
+    seg_carry_arrive<V, NV>(a, cur, chunk, l, lane, G, mask, col0, act, strm);
+  }
 }
 
 template <typename T, typename TC, int V, int NV, bool SEG>

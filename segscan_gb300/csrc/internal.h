@@ -84,6 +84,9 @@ struct EbGeom {
 };
 
 size_t eb_workspace_bytes(const EbGeom &g, int N);
+// segment SR: the element-balanced workspace plus the straddling segments'
+// element counts (2 ints per chunk, after eb_workspace_bytes)
+size_t seg_sr_workspace_bytes(const EbGeom &g, int N);
 // Sequential-walk geometry from knobs (abi.cu): worker_units scales
 // block_factor (nrow for SpMM, nnz for segments); val_bytes 0 for segments.
 ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_bytes, const ss_knobs &k, EbGeom &g);

@@ -57,6 +57,26 @@ def test_reductions(cuda, strategy, reduce, N):
     check(got, ref, dabs, reduce, 1e-5, f"{strategy} {reduce} N={N}")
 
 
+@pytest.mark.parametrize("reduce", ["sum", "max", "mean"])
+def test_sr_many_tiles_and_long_runs(cuda, reduce):
+    """SR with 4-lane groups and 16-column tiles (4 tiles at N = 64) and
+    32-element chunks: segments of up to 4000 elements span over a hundred
+    chunks, so the walk's straddling-segment probes take many rounds and
+    every column tile assembles its own part of each segment.  Two runs
+    give the same bits whichever chunk finishes a segment last."""
+    from segscan_gb300 import api
+    csr = synth.powerlaw(20000, 10, 2.1, 1, 4000, seed=31)
+    index = csr.coo_rows()
+    src = synth.dense(csr.nnz, 64, seed=32)
+    k = api.make_knobs("ebsr", 64, group_factor=2, coarsen_factor=4, thread_nz=8, block_denom=1)
+    srcd, idxd = torch.from_numpy(src).cuda(), torch.from_numpy(index).cuda()
+    got = seg(srcd, idxd, csr.nrow, reduce, "sr", knobs=k)
+    again = seg(srcd, idxd, csr.nrow, reduce, "sr", knobs=k)
+    ref, dabs = oracle(src, index, csr.nrow, reduce)
+    check(got, ref, dabs, reduce, 1e-5, f"sr 4 tiles {reduce}")
+    assert np.array_equal(got, again)
+
+
 @pytest.mark.parametrize("strategy", ["pr", "sr"])
 @pytest.mark.parametrize("reduce", ["sum", "max", "mean"])
 def test_bf16_src(cuda, strategy, reduce):
