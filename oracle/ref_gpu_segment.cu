@@ -14,8 +14,14 @@
 //   segment_coo_sorted_sr<float, int, 2, 4, 8, 2, 16>, the variant
 //     new-cg/src/main.cu:54 runs (segscan.cuh:974-1008):
 //     segscan_sr_sorted_kernel<float, int, CoarsenFactor 2, ThreadNz 4, DtileSize 8>
+//   segment_coo<float, int, 5, 256, 5, 1, 16> (segscan.cuh:150-184,
+//     new-cg/src/main.cu:50): segscan_kernel<float, int, float4, 32, 32>
+//   segment_coo_new<float, int, 5, 256, 5, 2> (segscan.cuh:327-355,
+//     new-cg/src/main.cu:51): segscan_new_kernel<float, int, float4, 32>
 // segscan_sr_kernel reads index[] up to group_size - 1 entries past nnz
-// (segscan.cuh:402, 459); the caller pads the index buffer.
+// (segscan.cuh:402, 459), segscan_kernel up to tile_size - 1 (:31) and
+// segscan_new_kernel up to blockDim.x - 1 (:209); the caller pads the index
+// buffer.
 #include <cuda_runtime.h>
 #include <cooperative_groups.h>
 #include <cuda_fp16.h>
@@ -38,5 +44,11 @@ __global__ void ref_seg_sr_n64(const float *src, const int *index, const int nnz
 }
 __global__ void ref_seg_sorted_sr(const float *src, const int *index, const int nnz, const int N, float *dst) {
   segscan_sr_sorted_kernel<float, int, 2, 4, 8>(src, index, nnz, N, dst);
+}
+__global__ void ref_seg_pr_f4(const float *src, const int *index, const int nnz, const int N, float *dst) {
+  segscan_kernel<float, int, float4, 32, 32>(src, index, nnz, N, dst);
+}
+__global__ void ref_seg_new_f4(const float *src, const int *index, const int nnz, const int N, float *dst) {
+  segscan_new_kernel<float, int, float4, 32>(src, index, nnz, N, dst);
 }
 }

@@ -143,15 +143,18 @@ class DgKernels:
 
 
 class RefSegmentKernels:
-    """Two of the reference's segment_coo kernels (new-cg/include/segscan/
-    segscan.cuh): segment_coo_sr<float, int, 4, 256, 4, 1, 1, 16> and the
-    segment_coo_sorted_sr<float, int, 2, 4, 8, 2, 16> that new-cg/src/main.cu
-    runs, with their launchers' geometry (segscan.cuh:817-829, 974-981).
-    Both add into dst, which the caller zeroes.  segscan_sr_kernel reads
-    index[] up to 15 entries past nnz (segscan.cuh:402, 459): `launch`
-    requires an index buffer padded by at least PAD entries."""
+    """Four of the reference's segment_coo kernels (new-cg/include/segscan/
+    segscan.cuh), each with its launcher's geometry:
+      sr      segment_coo_sr<float, int, 4, 256, 4, 1, 1, 16> (:817-829)
+      sorted  segment_coo_sorted_sr<float, int, 2, 4, 8, 2, 16> (:974-981), the one
+              new-cg/src/main.cu runs
+      pr      segment_coo<float, int, 5, 256, 5, 1, 16> (:150-171)
+      new     segment_coo_new<float, int, 5, 256, 5, 2> (:327-342)
+    All add into dst, which the caller zeroes.  They read index[] past nnz
+    (up to 15, 31 and blockDim.x - 1 = 127 entries: :402, :31, :209):
+    `launch` requires an index buffer padded by at least PAD entries."""
 
-    PAD = 32
+    PAD = 256
 
     def __init__(self):
         torch.cuda.init()
@@ -160,7 +163,7 @@ class RefSegmentKernels:
         self.mod = ctypes.c_void_p()
         RefKernels._check(self.cu.cuModuleLoad(ctypes.byref(self.mod), str(SEG_CUBIN).encode()), "cuModuleLoad")
         self.fn = {}
-        for name in ("ref_seg_sr_n64", "ref_seg_sorted_sr"):
+        for name in ("ref_seg_sr_n64", "ref_seg_sorted_sr", "ref_seg_pr_f4", "ref_seg_new_f4"):
             f = ctypes.c_void_p()
             RefKernels._check(self.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name.encode()), name)
             self.fn[name] = f
@@ -181,6 +184,20 @@ class RefSegmentKernels:
             grid, block, smem, fn = (ceil_div(N, bx * 2), ceil_div(nnz, by * 4), 1), (bx, by, 1), 0, "ref_seg_sorted_sr"
             if grid[1] > 65535:
                 raise ValueError(f"segment_coo_sorted_sr's grid.y {grid[1]} exceeds 65535 (nnz {nnz})")
+        elif which == "pr":  # float4, tile 32, 256 threads, block_factor 1/16
+            assert N % 4 == 0
+            ndim_warp = min(N, 32) // 4
+            nnz_warp_per_tb = ceil_div(256 // 32, ndim_warp)
+            workers = int(nnz * (1.0 / 16.0))
+            grid = (max(1, ceil_div(workers, nnz_warp_per_tb)), ceil_div(N, 32), 1)
+            block, smem, fn = (ndim_warp * 32, nnz_warp_per_tb, 1), 0, "ref_seg_pr_f4"
+        elif which == "new":  # float4, tile 32, 256 threads, blockDimY 2
+            assert N % 4 == 0
+            tiles_y = ceil_div(N, 4)
+            by = min(tiles_y, 2)  # blockDimY 2 is below 256 / tile = 8
+            bx = ceil_div(256, by)
+            grid, block, smem, fn = (ceil_div(nnz, bx), ceil_div(tiles_y, by), 1), (bx, by, 1), 0, "ref_seg_new_f4"
+            assert bx <= self.PAD
         else:
             raise ValueError(which)
         vals = [ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(index_padded.data_ptr()), ctypes.c_int(nnz),

@@ -120,7 +120,7 @@ def padded_index(index: np.ndarray) -> torch.Tensor:
 
 
 @seg_available
-@pytest.mark.parametrize("which", ["sr", "sorted"])
+@pytest.mark.parametrize("which", ["sr", "sorted", "pr", "new"])
 def test_reference_segment_kernels_match_ours(ref_seg, which):
     import oracle_lib
     csr = synth.powerlaw(30000, 30000, 2.1, 1, 3000, seed=24)
@@ -129,7 +129,8 @@ def test_reference_segment_kernels_match_ours(ref_seg, which):
     srcd = torch.from_numpy(src).cuda()
     dst_ref = torch.zeros((csr.nrow, 64), device="cuda")
     ref_seg.launch(which, srcd, padded_index(index), csr.nnz, dst_ref)
-    dst_ours = api.segment(srcd, torch.from_numpy(index).cuda(), csr.nrow, "sum")
+    dst_ours = api.segment(srcd, torch.from_numpy(index).cuda(), csr.nrow, "sum",
+                           "pr" if which in ("pr", "new") else "sr")
     torch.cuda.synchronize()
     d64, dabs = oracle_lib.segment_coo_f64(src, index, csr.nrow, 0)
     check_close(dst_ref.cpu().numpy(), d64, dabs, 1e-5, None, f"reference segment_coo {which} vs FP64")
@@ -151,7 +152,7 @@ def test_reference_segment_timings(ref_seg, capsys):
     dst = torch.empty((dst_len, 64), device="cuda")
     nbytes = synth.segment_bytes(nnz, 64, dst_len)
     rows = {}
-    for which in ("sr", "sorted"):
+    for which in ("sr", "sorted", "pr", "new"):
         def run():
             dst.zero_()
             ref_seg.launch(which, srcd, idx_pad, nnz, dst)
@@ -159,9 +160,13 @@ def test_reference_segment_timings(ref_seg, capsys):
         rows[f"reference_{which}"] = {"ms": t, "GB/s": nbytes / t / 1e6}
     ws_n = api.segment_workspace_size(nnz, 64, "sr")
     t_ours = _ms(lambda: api.segment(srcd, idx, dst_len, "sum", "sr", out=dst))
+    t_pr = _ms(lambda: api.segment(srcd, idx, dst_len, "sum", "pr", out=dst))
     best_ref = min(r["ms"] for r in rows.values())
     rows["ours_sr"] = {"ms": t_ours, "GB/s": nbytes / t_ours / 1e6, "speedup_vs_best_reference": best_ref / t_ours,
                        "workspace_bytes": ws_n}
+    # this library's PR family at the reference's segment_coo tuple (5,256,5,1,16)
+    rows["ours_pr"] = {"ms": t_pr, "GB/s": nbytes / t_pr / 1e6,
+                       "speedup_vs_reference_pr": rows["reference_pr"]["ms"] / t_pr}
     with capsys.disabled():
         print("\nreference_segment_kernels_sm103a " + json.dumps(rows))
     assert all(r["ms"] > 0 for r in rows.values())
