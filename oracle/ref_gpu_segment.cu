@@ -18,6 +18,10 @@
 //     new-cg/src/main.cu:50): segscan_kernel<float, int, float4, 32, 32>
 //   segment_coo_new<float, int, 5, 256, 5, 2> (segscan.cuh:327-355,
 //     new-cg/src/main.cu:51): segscan_new_kernel<float, int, float4, 32>
+//   segment_coo_noshmem_sr<float, int, 4, 256, 4, 2, 1, 16> (:868-916,
+//     main.cu:53): segscan_sr_noshmem_kernel<float, int, 4, 2, 16>
+//   segment_coo_noshmem_lessatom_sr<float, int, 4, 256, 4, 1, 1, 16>
+//     (:918-972, main.cu:54): segscan_sr_noshmem_lessatom_kernel<float, int, 4, 1, 16>
 // segscan_sr_kernel reads index[] up to group_size - 1 entries past nnz
 // (segscan.cuh:402, 459), segscan_kernel up to tile_size - 1 (:31) and
 // segscan_new_kernel up to blockDim.x - 1 (:209); the caller pads the index
@@ -50,5 +54,11 @@ __global__ void ref_seg_pr_f4(const float *src, const int *index, const int nnz,
 }
 __global__ void ref_seg_new_f4(const float *src, const int *index, const int nnz, const int N, float *dst) {
   segscan_new_kernel<float, int, float4, 32>(src, index, nnz, N, dst);
+}
+__global__ void ref_seg_noshmem_n64(const float *src, const int *index, const int nnz, const int N, float *dst) {
+  segscan_sr_noshmem_kernel<float, int, 4, 2, 16>(src, index, nnz, N, dst);
+}
+__global__ void ref_seg_lessatom_n64(const float *src, const int *index, const int nnz, const int N, float *dst) {
+  segscan_sr_noshmem_lessatom_kernel<float, int, 4, 1, 16>(src, index, nnz, N, dst);
 }
 }

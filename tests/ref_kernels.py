@@ -150,6 +150,8 @@ class RefSegmentKernels:
               new-cg/src/main.cu runs
       pr      segment_coo<float, int, 5, 256, 5, 1, 16> (:150-171)
       new     segment_coo_new<float, int, 5, 256, 5, 2> (:327-342)
+      noshmem segment_coo_noshmem_sr<float, int, 4, 256, 4, 2, 1, 16> (:868-880)
+      lessatom segment_coo_noshmem_lessatom_sr<float, int, 4, 256, 4, 1, 1, 16> (:918-930)
     All add into dst, which the caller zeroes.  They read index[] past nnz
     (up to 15, 31 and blockDim.x - 1 = 127 entries: :402, :31, :209):
     `launch` requires an index buffer padded by at least PAD entries."""
@@ -163,7 +165,8 @@ class RefSegmentKernels:
         self.mod = ctypes.c_void_p()
         RefKernels._check(self.cu.cuModuleLoad(ctypes.byref(self.mod), str(SEG_CUBIN).encode()), "cuModuleLoad")
         self.fn = {}
-        for name in ("ref_seg_sr_n64", "ref_seg_sorted_sr", "ref_seg_pr_f4", "ref_seg_new_f4"):
+        for name in ("ref_seg_sr_n64", "ref_seg_sorted_sr", "ref_seg_pr_f4", "ref_seg_new_f4", "ref_seg_noshmem_n64",
+                     "ref_seg_lessatom_n64"):
             f = ctypes.c_void_p()
             RefKernels._check(self.cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name.encode()), name)
             self.fn[name] = f
@@ -191,6 +194,9 @@ class RefSegmentKernels:
             workers = int(nnz * (1.0 / 16.0))
             grid = (max(1, ceil_div(workers, nnz_warp_per_tb)), ceil_div(N, 32), 1)
             block, smem, fn = (ndim_warp * 32, nnz_warp_per_tb, 1), 0, "ref_seg_pr_f4"
+        elif which in ("noshmem", "lessatom"):  # group 16, 256 threads, CoarsenFactor 4, block_factor 1/16
+            assert N == 64
+            grid, block, smem, fn = (int(nnz / 16), ceil_div(N, 16 * 4), 1), (256, 1, 1), 0, f"ref_seg_{which}_n64"
         elif which == "new":  # float4, tile 32, 256 threads, blockDimY 2
             assert N % 4 == 0
             tiles_y = ceil_div(N, 4)

@@ -120,7 +120,7 @@ def padded_index(index: np.ndarray) -> torch.Tensor:
 
 
 @seg_available
-@pytest.mark.parametrize("which", ["sr", "sorted", "pr", "new"])
+@pytest.mark.parametrize("which", ["sr", "sorted", "pr", "new", "noshmem", "lessatom"])
 def test_reference_segment_kernels_match_ours(ref_seg, which):
     import oracle_lib
     csr = synth.powerlaw(30000, 30000, 2.1, 1, 3000, seed=24)
@@ -152,7 +152,7 @@ def test_reference_segment_timings(ref_seg, capsys):
     dst = torch.empty((dst_len, 64), device="cuda")
     nbytes = synth.segment_bytes(nnz, 64, dst_len)
     rows = {}
-    for which in ("sr", "sorted", "pr", "new"):
+    for which in ("sr", "sorted", "pr", "new", "noshmem", "lessatom"):
         def run():
             dst.zero_()
             ref_seg.launch(which, srcd, idx_pad, nnz, dst)
