@@ -163,6 +163,68 @@ def spmm(A: CsrMatrix, B: torch.Tensor, strategy: str = "ebsr", knobs: Optional[
     return out
 
 
+class SpmmPlan:
+    """One SpMM shape bound once, for launch-bound loops (small matrices
+    called many times, as in a serving or training step).
+
+    The descriptor, knobs, workspace and stream are resolved here, so run()
+    is one C call (ss_spmm) after a shape and dtype check.  spmm() redoes
+    that work on every call: measured on GB300 with a 4096-row matrix, a
+    loop of spmm() costs 15 us of host time per call, of run() 3.8 us, and
+    of replays of the graph capture() records 2.0 us, against kernels of
+    6-12 us.  The plan keeps A's tensors and its workspace alive; the caller
+    keeps B and out alive across replays of a captured graph."""
+
+    def __init__(self, A: CsrMatrix, N: int, strategy: str = "ebsr", knobs: Optional[SsKnobs] = None,
+                 out_dtype: torch.dtype = torch.float32, accumulate: bool = False, stream=None):
+        self.A = A
+        self.N = int(N)
+        self.strategy = strategy
+        self.knobs = knobs if knobs is not None else default_knobs(strategy, self.N)
+        self.out_dtype = out_dtype
+        self.B_dtype = A.dtype
+        self._descr = A.descr()
+        dev = A.indptr.device
+        self.workspace = _workspace(spmm_workspace_size(A, self.N, strategy, self.knobs), dev)
+        wp, wn = _aligned(self.workspace)
+        self._stream = _stream(stream)
+        self._fn = _lib.load().ss_spmm
+        self._head = (int(STRATEGIES[strategy]), ctypes.byref(self._descr), self.N)
+        self._tail = (int(dtype_code(out_dtype)), int(bool(accumulate)), ctypes.byref(self.knobs), wp, wn,
+                      self._stream)
+        self._bshape = (A.ncol, self.N)
+        self._cshape = (A.nrow, self.N)
+        self.graph = None
+
+    def run(self, B: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+        """out = A @ B (or += with accumulate) on the plan's stream."""
+        if B.shape != self._bshape or out.shape != self._cshape or B.dtype != self.B_dtype \
+                or out.dtype != self.out_dtype or not (B.is_cuda and out.is_cuda):
+            raise ValueError(f"plan is for B {self._bshape} {self.B_dtype} and out {self._cshape} "
+                             f"{self.out_dtype} on the device")
+        rc = self._fn(*self._head, B.data_ptr(), out.data_ptr(), *self._tail)
+        if rc:
+            _lib.check(rc)
+        return out
+
+    def capture(self, B: torch.Tensor, out: torch.Tensor) -> "torch.cuda.CUDAGraph":
+        """Records run(B, out) into a CUDA graph (replay with .replay())."""
+        self.run(B, out)  # validates the arguments outside the capture
+        s = torch.cuda.Stream(device=out.device)
+        s.wait_stream(torch.cuda.current_stream(out.device))
+        g = torch.cuda.CUDAGraph()
+        saved = self._tail
+        self._tail = saved[:-1] + (s.cuda_stream,)
+        try:
+            with torch.cuda.graph(g, stream=s):
+                self.run(B, out)
+        finally:
+            self._tail = saved
+        torch.cuda.current_stream(out.device).wait_stream(s)
+        self.graph = g
+        return g
+
+
 def segment_workspace_size(nnz: int, N: int, strategy: str = "sr", knobs: Optional[SsKnobs] = None) -> int:
     n = ctypes.c_size_t()
     _lib.call("ss_segment_coo_workspace_size", int(SEG_STRATEGIES[strategy]), nnz, N,

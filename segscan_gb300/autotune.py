@@ -45,9 +45,9 @@ def features(A: api.CsrMatrix) -> dict:
             "frac_long": float((lengths > 32).sum()) / M}
 
 
-# bumped whenever the candidate list changes, so cached picks from an older
-# list are measured again
-CANDIDATES_REV = 2
+# bumped whenever the candidate list or the way candidates are timed
+# changes, so cached picks made the old way are measured again
+CANDIDATES_REV = 3
 
 
 def signature(A: api.CsrMatrix, N: int, f: Optional[dict] = None) -> str:
@@ -114,15 +114,17 @@ def _store_disk(key: str, val: dict) -> None:
 
 
 def time_candidate(A: api.CsrMatrix, B: torch.Tensor, strategy: str, knobs: SsKnobs, iters: int = 5) -> float:
+    """Device ms per call, timed through an SpmmPlan: api.spmm's ~15 us of
+    host work per call would hide the kernels of small matrices and make
+    every candidate look alike."""
     out = torch.empty((A.nrow, B.shape[1]), dtype=torch.float32, device=B.device)
-    ws_bytes = api.spmm_workspace_size(A, B.shape[1], strategy, knobs)
-    ws = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=B.device) if ws_bytes else None
-    api.spmm(A, B, strategy, knobs=knobs, out=out, workspace=ws)
+    plan = api.SpmmPlan(A, int(B.shape[1]), strategy, knobs)
+    plan.run(B, out)
     s = torch.cuda.current_stream(B.device)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
     for _ in range(iters):
-        api.spmm(A, B, strategy, knobs=knobs, out=out, workspace=ws)
+        plan.run(B, out)
     e1.record(s)
     e1.synchronize()
     return e0.elapsed_time(e1) / iters

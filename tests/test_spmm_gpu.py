@@ -310,3 +310,29 @@ def test_empty_row_runs(cuda, strategy, accumulate):
         ref = C64 + C0 if accumulate else C64
         check_close(out.cpu().numpy(), ref, absC + (np.abs(C0) if accumulate else 0), 1e-5, None,
                     f"{strategy} {kw} acc={accumulate}")
+
+
+@pytest.mark.parametrize("strategy", ["ebsr", "ebpr", "rbsr", "rbpr"])
+def test_plan_run_and_graph_match_spmm(cuda, strategy):
+    """SpmmPlan.run and its captured CUDA graph give the same bits as
+    api.spmm; a wrong shape or dtype is refused."""
+    from segscan_gb300 import api
+    A = synth.poisson(4096, 4096, 16.0, seed=5)
+    Ad = api.CsrMatrix.from_host(A, "cuda")
+    B = torch.from_numpy(synth.dense(A.ncol, 16, seed=6)).cuda()
+    ref = api.spmm(Ad, B, strategy)
+    plan = api.SpmmPlan(Ad, 16, strategy)
+    out = torch.full_like(ref, float("nan"))
+    plan.run(B, out)
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    out2 = torch.full_like(ref, float("nan"))
+    g = plan.capture(B, out2)
+    out2.fill_(float("nan"))
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out2, ref)
+    with pytest.raises(ValueError):
+        plan.run(B[:, :8].contiguous(), out)
+    with pytest.raises(ValueError):
+        plan.run(B.to(torch.bfloat16), out)
