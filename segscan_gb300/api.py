@@ -163,7 +163,35 @@ def spmm(A: CsrMatrix, B: torch.Tensor, strategy: str = "ebsr", knobs: Optional[
     return out
 
 
-class SpmmPlan:
+class _Plan:
+    """A bound call: run() validates and makes one C call whose last argument
+    is the stream handle; capture() records it into a CUDA graph."""
+
+    _tail: tuple
+
+    def run(self, *tensors):  # pragma: no cover - defined by subclasses
+        raise NotImplementedError
+
+    def capture(self, *tensors) -> "torch.cuda.CUDAGraph":
+        """Records run(*tensors) into a CUDA graph (replay with .replay())."""
+        self.run(*tensors)  # validates the arguments outside the capture
+        dev = tensors[-1].device
+        s = torch.cuda.Stream(device=dev)
+        s.wait_stream(torch.cuda.current_stream(dev))
+        g = torch.cuda.CUDAGraph()
+        saved = self._tail
+        self._tail = saved[:-1] + (s.cuda_stream,)
+        try:
+            with torch.cuda.graph(g, stream=s):
+                self.run(*tensors)
+        finally:
+            self._tail = saved
+        torch.cuda.current_stream(dev).wait_stream(s)
+        self.graph = g
+        return g
+
+
+class SpmmPlan(_Plan):
     """One SpMM shape bound once, for launch-bound loops (small matrices
     called many times, as in a serving or training step).
 
@@ -184,14 +212,12 @@ class SpmmPlan:
         self.out_dtype = out_dtype
         self.B_dtype = A.dtype
         self._descr = A.descr()
-        dev = A.indptr.device
-        self.workspace = _workspace(spmm_workspace_size(A, self.N, strategy, self.knobs), dev)
+        self.workspace = _workspace(spmm_workspace_size(A, self.N, strategy, self.knobs), A.indptr.device)
         wp, wn = _aligned(self.workspace)
-        self._stream = _stream(stream)
         self._fn = _lib.load().ss_spmm
         self._head = (int(STRATEGIES[strategy]), ctypes.byref(self._descr), self.N)
         self._tail = (int(dtype_code(out_dtype)), int(bool(accumulate)), ctypes.byref(self.knobs), wp, wn,
-                      self._stream)
+                      _stream(stream))
         self._bshape = (A.ncol, self.N)
         self._cshape = (A.nrow, self.N)
         self.graph = None
@@ -207,22 +233,45 @@ class SpmmPlan:
             _lib.check(rc)
         return out
 
-    def capture(self, B: torch.Tensor, out: torch.Tensor) -> "torch.cuda.CUDAGraph":
-        """Records run(B, out) into a CUDA graph (replay with .replay())."""
-        self.run(B, out)  # validates the arguments outside the capture
-        s = torch.cuda.Stream(device=out.device)
-        s.wait_stream(torch.cuda.current_stream(out.device))
-        g = torch.cuda.CUDAGraph()
-        saved = self._tail
-        self._tail = saved[:-1] + (s.cuda_stream,)
-        try:
-            with torch.cuda.graph(g, stream=s):
-                self.run(B, out)
-        finally:
-            self._tail = saved
-        torch.cuda.current_stream(out.device).wait_stream(s)
-        self.graph = g
-        return g
+
+class SegmentPlan(_Plan):
+    """segment_coo over one sorted index bound once (a GNN layer's
+    aggregation, called every step): the index, sizes, knobs, workspace and
+    stream are resolved here, run(src, out) is one C call and capture()
+    records it into a CUDA graph, as for SpmmPlan.  The plan keeps the
+    index and its workspace alive."""
+
+    def __init__(self, index: torch.Tensor, dst_len: int, N: int, reduce: str = "sum", strategy: str = "sr",
+                 src_dtype: torch.dtype = torch.float32, knobs: Optional[SsKnobs] = None, accumulate: bool = False,
+                 stream=None):
+        _need_cuda("index", index, torch.int32)
+        if index.dim() != 1:
+            raise ValueError("index must be 1-D")
+        self.index = index
+        self.nnz, self.N, self.dst_len = int(index.numel()), int(N), int(dst_len)
+        self.src_dtype = src_dtype
+        self.knobs = knobs
+        self.workspace = _workspace(segment_workspace_size(self.nnz, self.N, strategy, knobs), index.device)
+        wp, wn = _aligned(self.workspace)
+        self._fn = _lib.load().ss_segment_coo
+        self._seg = int(SEG_STRATEGIES[strategy])
+        self._mid = (int(dtype_code(src_dtype)), index.data_ptr(), self.nnz, self.N, self.dst_len)
+        self._tail = (int(REDUCES[reduce]), int(bool(accumulate)), ctypes.byref(knobs) if knobs is not None else None,
+                      wp, wn, _stream(stream))
+        self._sshape = (self.nnz, self.N)
+        self._dshape = (self.dst_len, self.N)
+        self.graph = None
+
+    def run(self, src: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+        """out[index[i], :] (op)= src[i, :] on the plan's stream."""
+        if src.shape != self._sshape or out.shape != self._dshape or src.dtype != self.src_dtype \
+                or out.dtype != torch.float32 or not (src.is_cuda and out.is_cuda):
+            raise ValueError(f"plan is for src {self._sshape} {self.src_dtype} and out {self._dshape} float32 "
+                             f"on the device")
+        rc = self._fn(self._seg, src.data_ptr(), *self._mid, out.data_ptr(), *self._tail)
+        if rc:
+            _lib.check(rc)
+        return out
 
 
 def segment_workspace_size(nnz: int, N: int, strategy: str = "sr", knobs: Optional[SsKnobs] = None) -> int:

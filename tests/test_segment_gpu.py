@@ -137,3 +137,26 @@ def test_index_validate(cuda):
     assert api.validate_index(idx, 5) == 0
     assert api.validate_index(idx, 4) & 32
     assert api.validate_index(torch.tensor([2, 1], dtype=torch.int32, device="cuda"), 5) & 16
+
+
+@pytest.mark.parametrize("strategy", ["sr", "pr"])
+@pytest.mark.parametrize("reduce", ["sum", "mean"])
+def test_segment_plan_and_graph_match(cuda, strategy, reduce):
+    """SegmentPlan.run and its CUDA graph give the same bits as api.segment."""
+    from segscan_gb300 import api
+    csr = synth.powerlaw(8000, 10, 2.1, 1, 500, seed=41)
+    index = torch.from_numpy(csr.coo_rows()).cuda()
+    src = torch.from_numpy(synth.dense(csr.nnz, 32, seed=42)).cuda()
+    ref = api.segment(src, index, csr.nrow, reduce, strategy)
+    plan = api.SegmentPlan(index, csr.nrow, 32, reduce, strategy)
+    out = torch.full_like(ref, float("nan"))
+    plan.run(src, out)
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    g = plan.capture(src, out)
+    out.fill_(float("nan"))
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    with pytest.raises(ValueError):
+        plan.run(src[:, :16].contiguous(), out)
