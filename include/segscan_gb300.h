@@ -197,6 +197,8 @@ ss_status ss_spmm(int strategy, const ss_csr *A, int N, const void *B,
 /* segment_coo: dst[index[i], :] (op)= src[i, :] over sorted index.    */
 /* ---------------------------------------------------------------- */
 
+/* Workspace bytes ss_segment_coo needs for nnz x N with these knobs, for
+ * any source dtype (the largest of the three). */
 ss_status ss_segment_coo_workspace_size(int seg_strategy, int nnz, int N,
                                         const ss_knobs *knobs, size_t *bytes);
 

@@ -484,10 +484,18 @@ ss_status ss_segment_coo_workspace_size(int seg_strategy, int nnz, int N, const 
   if (nnz < 0 || N < 0) return fail(SS_ERR_INVALID_ARG, "negative size");
   ss_knobs tmp;
   if (!knobs) { seg_default_knobs(seg_strategy, tmp); knobs = &tmp; }
-  EbGeom g;
-  ss_status st = seg_geometry(seg_strategy, nnz, N, SS_F32, *knobs, g);
-  if (st) return st;
-  *bytes = seg_strategy == SS_SEG_SR ? seg_sr_workspace_bytes(g, N) : eb_workspace_bytes(g, N);
+  // the query has no source dtype: the chunking depends on it (16-bit
+  // sources take wider vectors, so more, smaller chunks), so return the
+  // largest need over the three
+  size_t most = 0;
+  for (int dt : {SS_F32, SS_BF16, SS_F16}) {
+    EbGeom g;
+    ss_status st = seg_geometry(seg_strategy, nnz, N, dt, *knobs, g);
+    if (st) return st;
+    const size_t need = seg_strategy == SS_SEG_SR ? seg_sr_workspace_bytes(g, N) : eb_workspace_bytes(g, N);
+    if (need > most) most = need;
+  }
+  *bytes = most;
   return SS_OK;
 }
 
