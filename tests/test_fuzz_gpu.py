@@ -98,3 +98,57 @@ def test_segment_fuzz(cuda, seed):
         assert np.array_equal(got.astype(np.float64), ref), what
     else:
         check_close(got, ref, dabs, 1e-5, None, what)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_transpose_and_sddmm_fuzz(cuda, seed):
+    """Random matrices: the device transpose is bit-exact against a stable
+    argsort by column (pattern, permutation, gathered values), and SDDMM is
+    within 1e-5 of FP64 dot products."""
+    rng = np.random.default_rng(11000 + seed)
+    M, K = int(rng.integers(1, 5000)), int(rng.integers(1, 5000))
+    L, kind = lengths_for(rng, M, K)
+    A = synth.csr_from_lengths(M, K, L, rng)
+    Ad = api.CsrMatrix.from_host(A, "cuda")
+    AT, perm = api.transpose(Ad)
+    order = np.argsort(A.indices, kind="stable")
+    rows_of = np.repeat(np.arange(M, dtype=np.int32), np.diff(A.indptr))
+    exp_indptr = np.zeros(K + 1, np.int64)
+    np.cumsum(np.bincount(A.indices, minlength=K), out=exp_indptr[1:])
+    what = f"seed {seed}: M={M} K={K} nnz={A.nnz} kind={kind}"
+    assert np.array_equal(AT.indptr.cpu().numpy(), exp_indptr.astype(np.int32)), what
+    assert np.array_equal(AT.indices.cpu().numpy(), rows_of[order]), what
+    assert np.array_equal(perm.cpu().numpy(), order.astype(np.int32)), what
+    assert np.array_equal(AT.values.cpu().numpy(), A.values[order]), what
+    N = int(rng.choice(WIDTHS))
+    dC = synth.dense(M, N, seed=seed + 3)
+    B = synth.dense(K, N, seed=seed + 4)
+    got = api.sddmm(Ad, torch.from_numpy(dC).cuda(), torch.from_numpy(B).cuda()).cpu().numpy()
+    x = dC[rows_of].astype(np.float64) * B[A.indices].astype(np.float64)
+    check_close(got, x.sum(axis=1), np.abs(x).sum(axis=1), 1e-5, None, f"SDDMM {what} N={N}")
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_batched_fuzz(cuda, seed):
+    """Random batches (2-40 matrices of random shapes, widths and chunk
+    targets) in one persistent launch, each matrix against FP64."""
+    from segscan_gb300 import autotune, batched
+    rng = np.random.default_rng(13000 + seed)
+    count = int(rng.integers(2, 41))
+    N = int(rng.choice([1, 4, 8, 16, 32, 33, 64, 128]))
+    mats_h = []
+    for _ in range(count):
+        M, K = int(rng.integers(1, 3000)), int(rng.integers(1, 3000))
+        L, _ = lengths_for(rng, M, K)
+        mats_h.append(synth.csr_from_lengths(M, K, L, rng))
+    mats = [api.CsrMatrix.from_host(A, "cuda") for A in mats_h]
+    Bs_h = [synth.dense(A.ncol, N, seed=seed * 100 + i) for i, A in enumerate(mats_h)]
+    Bs = [torch.from_numpy(B).cuda() for B in Bs_h]
+    target = int(rng.choice([128, 256, 512, 1024]))
+    plan = batched.BatchedSpMM(mats, Bs, knobs=autotune.batch_knobs(mats, N, target))
+    plan.run()
+    torch.cuda.synchronize()
+    for i, (A, B) in enumerate(zip(mats_h, Bs_h)):
+        C64, absC = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B)
+        check_close(plan.out[i].cpu().numpy(), C64, absC, 1e-5, None,
+                    f"seed {seed}: matrix {i} of {count} ({A.nrow}x{A.ncol}, nnz {A.nnz}) N={N} target={target}")
