@@ -40,25 +40,33 @@ def spmm_case(seed):
     L, kind = lengths_for(rng, M, K)
     A = synth.csr_from_lengths(M, K, L, rng)
     N = int(rng.choice(WIDTHS))
-    bf16 = bool(rng.random() < 0.25)
+    dt = [torch.float32, torch.float32, torch.float32, torch.bfloat16, torch.float16][int(rng.integers(0, 5))]
     strategy = ["ebsr", "ebpr", "rbsr", "rbpr"][int(rng.integers(0, 4))]
-    acts = [k for s, k in sweep.library_actions(N, torch.bfloat16 if bf16 else torch.float32) if s == strategy]
+    acts = [k for s, k in sweep.library_actions(N, dt) if s == strategy]
     knobs = acts[int(rng.integers(0, len(acts)))]
     accumulate = bool(rng.random() < 0.2)
-    return A, N, bf16, strategy, knobs, accumulate, kind, rng
+    # C: FP32, or the 16-bit storage type, or (ebsr only) 16-bit from FP32 inputs
+    c16 = [torch.bfloat16, torch.float16][int(rng.integers(0, 2))] if dt == torch.float32 else dt
+    cdt = c16 if (rng.random() < 0.3 and (dt != torch.float32 or strategy == "ebsr")) else torch.float32
+    return A, N, dt, cdt, strategy, knobs, accumulate, kind, rng
+
+
+# one output rounding: half an ulp of the 16-bit type, relative (FP16 also
+# absolute for its subnormals)
+C_ROUND = {torch.float32: (0.0, 0.0), torch.bfloat16: (2.0 ** -8, 0.0), torch.float16: (2.0 ** -11, 2.0 ** -24)}
 
 
 @pytest.mark.parametrize("seed", range(64))
 def test_spmm_fuzz(cuda, seed):
-    A, N, bf16, strategy, knobs, accumulate, kind, rng = spmm_case(seed)
+    A, N, dt, cdt, strategy, knobs, accumulate, kind, rng = spmm_case(seed)
     B = synth.dense(A.ncol, N, seed=seed)
-    dt = torch.bfloat16 if bf16 else torch.float32
-    vals = rounded(A.values, dt) if bf16 else A.values
-    Bc = rounded(B, dt) if bf16 else B
+    vals = rounded(A.values, dt) if dt != torch.float32 else A.values
+    Bc = rounded(B, dt) if dt != torch.float32 else B
     Ad = api.CsrMatrix.from_host(A, "cuda", dt)
     Bd = torch.from_numpy(B).cuda().to(dt)
-    C0 = synth.dense(A.nrow, N, seed=seed + 1) if accumulate else None
-    out = torch.from_numpy(C0).cuda() if accumulate else torch.full((A.nrow, N), float("nan"), device="cuda")
+    C0 = rounded(synth.dense(A.nrow, N, seed=seed + 1), cdt) if accumulate else None
+    out = torch.from_numpy(C0).cuda().to(cdt) if accumulate else torch.full((A.nrow, N), float("nan"),
+                                                                             dtype=cdt, device="cuda")
     try:
         api.spmm(Ad, Bd, strategy, knobs=knobs, out=out, accumulate=accumulate)
     except api._lib.SegscanError as exc:  # a tuple the geometry rejects is refused, not computed
@@ -69,9 +77,10 @@ def test_spmm_fuzz(cuda, seed):
     if accumulate:
         C64 = C64 + C0
         absC = absC + np.abs(C0)
-    what = (f"seed {seed}: M={A.nrow} K={A.ncol} nnz={A.nnz} kind={kind} N={N} bf16={bf16} "
+    what = (f"seed {seed}: M={A.nrow} K={A.ncol} nnz={A.nnz} kind={kind} N={N} storage={dt} C={cdt} "
             f"{sweep.label(strategy, knobs)} accumulate={accumulate}")
-    check_close(out.cpu().numpy(), C64, absC, 1e-5, None, what)
+    rel, ab = C_ROUND[cdt]
+    check_close(out.float().cpu().numpy(), C64, absC + rel * np.abs(C64) / 1e-5, 1e-5, None, what, atol=ab)
 
 
 @pytest.mark.parametrize("seed", range(48))
