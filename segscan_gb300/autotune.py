@@ -47,7 +47,7 @@ def features(A: api.CsrMatrix) -> dict:
 
 # bumped whenever the candidate list or the way candidates are timed
 # changes, so cached picks made the old way are measured again
-CANDIDATES_REV = 3
+CANDIDATES_REV = 4
 
 
 def signature(A: api.CsrMatrix, N: int, f: Optional[dict] = None) -> str:
@@ -74,6 +74,13 @@ def candidates(N: int, dtype: torch.dtype = torch.float32) -> list[tuple[str, di
                 for tpb in (128, 256, 512):
                     c.append(("ebsr", dict(group_factor=gf, coarsen_factor=vec, thread_nz=tnz, block_denom=1,
                                            thread_per_block=tpb)))
+    # one lane per group (the narrow walk) holding eight elements of a row
+    # each: the fastest layout at N = 8 (the group walk wins from N = 16 up)
+    if 8 <= N <= 16:
+        for tnz in (32, 64):
+            for tpb in (128, 256, 512):
+                c.append(("ebsr", dict(group_factor=0, coarsen_factor=8, thread_nz=tnz, block_denom=1,
+                                       thread_per_block=tpb)))
     # small blocks spread a small matrix's rows over more SMs
     for cf, tf in ((4, 5), (4, 6), (2, 5), (2, 6)):
         for tpb in (128, 256):

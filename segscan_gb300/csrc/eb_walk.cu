@@ -77,6 +77,11 @@ ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
     cudaError_t e = cudaMemsetAsync(a.carry_cnt, 0, carry_rows_bytes(g.num_chunks, g.cs.tiles), s);
     if (e != cudaSuccess) return cuda_fail(e, "ebsr carry counts");
   }
+  // one lane per group: the narrow walk (eb_narrow.cu), no staging
+  if (g.cs.lanes == 1) {
+    void *nf = narrow_kernel(c.val_dtype, c.c_dtype, g.cs.V, g.cs.NV);
+    if (nf) return run_sr(nf, a, g, 0, s, "ebsr narrow launch");
+  }
   return run_sr(fn, a, g, sr_smem_bytes(g.stage, g.workers_per_block, dtype_size(c.val_dtype)), s, "ebsr launch");
 }
 

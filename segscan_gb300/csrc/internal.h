@@ -92,6 +92,9 @@ size_t seg_sr_workspace_bytes(const EbGeom &g, int N);
 ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_bytes, const ss_knobs &k, EbGeom &g);
 // shared memory of the sequential-walk kernels (eb_walk.cu)
 size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes);
+// ebsr with one lane per group (eb_narrow.cu): the kernel for these value /
+// output types and vector shape, or null
+void *narrow_kernel(int val_dtype, int c_dtype, int V, int NV);
 // device address of the bounded-wait status word (eb_walk.cu)
 int *walk_error_ptr();
 
