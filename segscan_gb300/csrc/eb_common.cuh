@@ -180,7 +180,7 @@ __device__ __forceinline__ void load_slot(const float *p, float (&out)[V]) {
 // row once - the same arithmetic, in the same order, as fixup_chunk, so the
 // result does not depend on which participant finishes last.  Nothing
 // waits: a participant that is not last returns at once.
-template <typename TC, int V, int NV>
+template <typename TC, int V, int NV, int BATCH = 1>
 __device__ __forceinline__ void carry_arrive(const EbArgs &a, int r, int lane, int G, unsigned mask, int col0,
                                           const bool (&act)[NV], uint64_t pol) {
   const int o = __ldg(a.indptr + r) / a.chunk;
@@ -202,10 +202,31 @@ __device__ __forceinline__ void carry_arrive(const EbArgs &a, int r, int lane, i
     load_slot<V>(a.tail_vals + (int64_t)o * a.N + col, acc);
     #pragma unroll
     for (int i = 0; i < V; i++) comp[i] = 0.f;
-    for (int k = o + 1; k <= l; k++) {
-      load_slot<V>(a.carry_vals + (int64_t)k * a.N + col, x);
-      #pragma unroll
-      for (int i = 0; i < V; i++) kahan_add(acc[i], comp[i], x[i]);
+    if constexpr (BATCH == 1) {
+      for (int k = o + 1; k <= l; k++) {
+        load_slot<V>(a.carry_vals + (int64_t)k * a.N + col, x);
+        #pragma unroll
+        for (int i = 0; i < V; i++) kahan_add(acc[i], comp[i], x[i]);
+      }
+    } else {  // BATCH heads in flight, added in the same order
+      for (int k0 = o + 1; k0 <= l; k0 += BATCH) {
+        float xb[BATCH][V];
+        #pragma unroll
+        for (int u = 0; u < BATCH; u++) {
+          if (k0 + u <= l) {
+            load_slot<V>(a.carry_vals + (int64_t)(k0 + u) * a.N + col, xb[u]);
+          } else {
+            #pragma unroll
+            for (int i = 0; i < V; i++) xb[u][i] = 0.f;
+          }
+        }
+        #pragma unroll
+        for (int u = 0; u < BATCH; u++) {
+          if (k0 + u > l) break;
+          #pragma unroll
+          for (int i = 0; i < V; i++) kahan_add(acc[i], comp[i], xb[u][i]);
+        }
+      }
     }
     TC *dst = C + (int64_t)r * a.N + col;
     if (a.accumulate) {

@@ -187,8 +187,10 @@ __global__ void __launch_bounds__(512) eb_narrow_kernel(EbArgs a) {
       }
     }
     // straddling rows: count this chunk in; the last participant stores
-    if (head >= 0) carry_arrive<TC, V, NV>(a, head, 0, 1, self, col0, act, strm);
-    if (tail >= 0) carry_arrive<TC, V, NV>(a, tail, 0, 1, self, col0, act, strm);
+    // (small chunks: a long row has hundreds of heads, so eight are loaded
+    // at a time)
+    if (head >= 0) carry_arrive<TC, V, NV, 8>(a, head, 0, 1, self, col0, act, strm);
+    if (tail >= 0) carry_arrive<TC, V, NV, 8>(a, tail, 0, 1, self, col0, act, strm);
   }
 }
 
