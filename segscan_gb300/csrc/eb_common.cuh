@@ -266,14 +266,21 @@ __device__ __forceinline__ int seg_probe_fwd(const EbArgs &a, int chunk, int lan
 }
 
 // Owner chunk of segment r, which continues into `chunk` from before it;
-// `back` is this lane's seg_probe_back(chunk).
+// `back` is this lane's seg_probe_back(chunk).  The nearest chunk j before
+// `chunk` whose first id is below r holds r's start unless r starts exactly
+// at chunk j + 1's first element (then j + 1 owns it): the last id of
+// chunk j tells which.
 __device__ __forceinline__ int seg_owner(const EbArgs &a, int r, int chunk, int back, int lane, int G,
                                          unsigned mask) {
   int base = chunk - 1;  // lane i holds the first id of chunk base - i
   int v = back;
   while (true) {
     const unsigned m = group_ballot(mask, v < r, G);
-    if (m) return max(base - (__ffs(m) - 1), 0);  // a probe before the array: r starts at 0
+    if (m) {
+      const int j = base - (__ffs(m) - 1);
+      if (j < 0) return 0;  // a probe before the array: r starts at element 0
+      return __ldg(a.index + (int64_t)(j + 1) * a.chunk - 1) == r ? j : j + 1;
+    }
     base -= G;  // every probe was r: r started before all of them (base >= G here)
     v = seg_probe_back(a, base + 1, lane);
   }

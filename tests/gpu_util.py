@@ -20,7 +20,7 @@ def check_close(C, C64, absC, rtol, normwise=None, what="", atol=1e-30):
     C = np.asarray(C, dtype=np.float64)
     err = np.abs(C - C64)
     bound = rtol * absC + atol
-    bad = err > bound
+    bad = ~(err <= bound)  # NaN (an element never written, or computed as NaN) counts as off
     assert not bad.any(), (f"{what}: {bad.sum()} elements off; worst err {err.max():.3e} "
                            f"at {np.unravel_index(np.argmax(err - bound), err.shape)}")
     if normwise is not None:

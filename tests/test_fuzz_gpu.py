@@ -97,7 +97,8 @@ def test_segment_fuzz(cuda, seed):
     src = synth.dense(index.size, N, seed=seed)
     dt = torch.bfloat16 if bf16 else torch.float32
     srcd = torch.from_numpy(src).cuda().to(dt)
-    out = api.segment(srcd, torch.from_numpy(index).cuda(), dst_len, reduce, strategy)
+    out = torch.full((dst_len, N), float("nan"), device="cuda")  # a row nobody stores shows up
+    api.segment(srcd, torch.from_numpy(index).cuda(), dst_len, reduce, strategy, out=out)
     torch.cuda.synchronize()
     ref, dabs = oracle_lib.segment_coo_f64(rounded(src, dt) if bf16 else src, index, dst_len,
                                            {"sum": 0, "max": 1, "mean": 2}[reduce])

@@ -17,6 +17,8 @@ REDUCE = {"sum": 0, "max": 1, "mean": 2}
 
 def seg(src, index, dst_len, reduce, strategy, **kw):
     from segscan_gb300 import api
+    if "out" not in kw:  # NaN first: a row the kernel never stores shows up
+        kw["out"] = torch.full((dst_len, src.shape[1]), float("nan"), device=src.device)
     out = api.segment(src, index, dst_len, reduce, strategy, **kw)
     torch.cuda.synchronize()
     return out.cpu().numpy()
@@ -160,3 +162,25 @@ def test_segment_plan_and_graph_match(cuda, strategy, reduce):
     assert torch.equal(out, ref)
     with pytest.raises(ValueError):
         plan.run(src[:, :16].contiguous(), out)
+
+
+@pytest.mark.parametrize("reduce", ["sum", "max", "mean"])
+@pytest.mark.parametrize("knobs_kw,chunk", [(dict(group_factor=2, thread_nz=8), 32),
+                                            (dict(group_factor=4, thread_nz=8), 128)])
+def test_sr_segments_starting_on_chunk_boundaries(cuda, reduce, knobs_kw, chunk):
+    """Every segment starts exactly at a chunk boundary and most span several
+    chunks: the owner of such a segment is the chunk it starts in, not the
+    one before.  dst starts as NaN, so a segment nobody stores shows up."""
+    from segscan_gb300 import api
+    rng = np.random.default_rng(91 + chunk)
+    lengths = chunk * rng.integers(1, 41, size=300)
+    index = np.repeat(np.arange(lengths.size, dtype=np.int32), lengths)
+    dst_len = lengths.size + 2
+    src = synth.dense(index.size, 64, seed=92)
+    k = api.make_knobs("ebsr", 64, coarsen_factor=4, block_denom=1, **knobs_kw)
+    out = torch.full((dst_len, 64), float("nan"), device="cuda")
+    api.segment(torch.from_numpy(src).cuda(), torch.from_numpy(index).cuda(), dst_len, reduce, "sr", knobs=k,
+                out=out)
+    torch.cuda.synchronize()
+    ref, dabs = oracle(src, index, dst_len, reduce)
+    check(out.cpu().numpy(), ref, dabs, reduce, 1e-5, f"segments on {chunk}-element boundaries, {reduce}")

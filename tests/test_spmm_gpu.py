@@ -336,3 +336,53 @@ def test_plan_run_and_graph_match_spmm(cuda, strategy):
         plan.run(B[:, :8].contiguous(), out)
     with pytest.raises(ValueError):
         plan.run(B.to(torch.bfloat16), out)
+
+
+def test_concurrent_streams_and_threads(cuda):
+    """The C ABI is stream-ordered and reentrant: four host threads, each
+    with its own stream, matrix and workspace, call SpMM and segment_coo
+    concurrently (ctypes releases the GIL during the calls); every result
+    matches FP64, and the per-thread last-error message stays per thread."""
+    import threading
+    from segscan_gb300 import api
+    jobs = []
+    for t in range(4):
+        A = synth.powerlaw(20000 + 1000 * t, 20000, 2.1, 1, 2000, seed=60 + t)
+        B = synth.dense(A.ncol, 32, seed=70 + t)
+        jobs.append((A, B, ["ebsr", "ebpr", "rbsr", "rbpr"][t]))
+    results, errors = [None] * 4, []
+
+    def work(t):
+        try:
+            A, B, strategy = jobs[t]
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                Ad = api.CsrMatrix.from_host(A, "cuda")
+                Bd = torch.from_numpy(B).cuda()
+                idx = torch.from_numpy(A.coo_rows()).cuda()
+                src = torch.from_numpy(synth.dense(A.nnz, 8, seed=80 + t)).cuda()
+                for _ in range(20):
+                    C = api.spmm(Ad, Bd, strategy, stream=s)
+                    seg = api.segment(src, idx, A.nrow, "sum", stream=s)
+                try:  # an invalid call on this thread: its message is this thread's
+                    api.spmm(Ad, Bd[:, :7].contiguous(), strategy, knobs=api.make_knobs(strategy, 7, thread_per_block=4096))
+                except api._lib.SegscanError as exc:
+                    msg = str(exc)
+                s.synchronize()
+                results[t] = (C.cpu().numpy(), seg.cpu().numpy(), src.cpu().numpy(), msg)
+        except Exception as exc:  # surfaced in the main thread
+            errors.append(exc)
+
+    threads = [threading.Thread(target=work, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for t, (A, B, strategy) in enumerate(jobs):
+        C, seg, src, msg = results[t]
+        C64, absC = oracle64(A, B)
+        check_close(C, C64, absC, 1e-5, None, f"thread {t} {strategy}")
+        d64, dabs = oracle_lib.segment_coo_f64(src, A.coo_rows(), A.nrow, 0)
+        check_close(seg, d64, dabs, 1e-5, None, f"thread {t} segment")
+        assert "thread_per_block" in msg, msg
