@@ -116,6 +116,13 @@ def make_knobs(strategy: str, N: int = 64, **kw) -> SsKnobs:
     return k
 
 
+def _output(shape, dtype: torch.dtype, device) -> torch.Tensor:
+    """A result tensor the library's kernels fill (every allocation of an
+    output goes through here; the tests poison it to catch unwritten
+    elements)."""
+    return torch.empty(shape, dtype=dtype, device=device)
+
+
 def _workspace(nbytes: int, device) -> Optional[torch.Tensor]:
     if nbytes == 0:
         return None
@@ -149,7 +156,7 @@ def spmm(A: CsrMatrix, B: torch.Tensor, strategy: str = "ebsr", knobs: Optional[
     N = int(B.shape[1])
     cdt = out_dtype or (out.dtype if out is not None else torch.float32)
     if out is None:
-        out = torch.empty((A.nrow, N), dtype=cdt, device=B.device)
+        out = _output((A.nrow, N), cdt, B.device)
     _need_cuda("out", out, cdt)
     if tuple(out.shape) != (A.nrow, N):
         raise ValueError(f"out must be [{A.nrow}, {N}]")
@@ -291,7 +298,7 @@ def segment(src: torch.Tensor, index: torch.Tensor, dst_len: int, reduce: str = 
     _need_cuda("index", index, torch.int32)
     nnz, N = int(src.shape[0]), int(src.shape[1])
     if out is None:
-        out = torch.empty((dst_len, N), dtype=torch.float32, device=src.device)
+        out = _output((dst_len, N), torch.float32, src.device)
     _need_cuda("out", out, torch.float32)
     ws = _workspace(segment_workspace_size(nnz, N, strategy, knobs), src.device)
     wp, wn = _aligned(ws)
@@ -306,7 +313,7 @@ def row_ids(indptr: torch.Tensor, nnz: int, elems: Optional[torch.Tensor] = None
     _need_cuda("indptr", indptr, torch.int32)
     M = int(indptr.numel()) - 1
     count = nnz if elems is None else int(elems.numel())
-    rows = torch.empty(count, dtype=torch.int32, device=indptr.device)
+    rows = _output(count, torch.int32, indptr.device)
     if elems is not None:
         _need_cuda("elems", elems, torch.int32)
     _lib.call("ss_row_ids", _ptr(indptr), M, nnz, _ptr(elems), count, _ptr(rows), _stream(stream))
@@ -433,9 +440,9 @@ def transpose(A: CsrMatrix, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
     _lib.call("ss_csr_transpose_workspace_size", ctypes.byref(d), ctypes.byref(n))
     ws = _workspace(int(n.value), dev)
     wp, wn = _aligned(ws)
-    t_indptr = torch.empty(A.ncol + 1, dtype=torch.int32, device=dev)
-    t_indices = torch.empty(A.nnz, dtype=torch.int32, device=dev)
-    perm = torch.empty(A.nnz, dtype=torch.int32, device=dev)
+    t_indptr = _output(A.ncol + 1, torch.int32, dev)
+    t_indices = _output(A.nnz, torch.int32, dev)
+    perm = _output(A.nnz, torch.int32, dev)
     _lib.call("ss_csr_transpose", ctypes.byref(d), _ptr(t_indptr), _ptr(t_indices), _ptr(perm), wp, wn,
               _stream(stream))
     vals = None
@@ -459,9 +466,9 @@ def coo_to_csr(nrow: int, rows: torch.Tensor, cols: torch.Tensor, ncol: Optional
     _lib.call("ss_coo_to_csr_workspace_size", nrow, nnz, ctypes.byref(n))
     ws = _workspace(int(n.value), dev)  # held until the launches are queued: the
     wp, wn = _aligned(ws)                # allocator must not hand it to the outputs below
-    indptr = torch.empty(nrow + 1, dtype=torch.int32, device=dev)
-    out_cols = torch.empty(nnz, dtype=torch.int32, device=dev)
-    perm = torch.empty(nnz, dtype=torch.int32, device=dev)
+    indptr = _output(nrow + 1, torch.int32, dev)
+    out_cols = _output(nnz, torch.int32, dev)
+    perm = _output(nnz, torch.int32, dev)
     _lib.call("ss_coo_to_csr", nrow, nnz, _ptr(rows), _ptr(cols), _ptr(indptr), _ptr(out_cols), _ptr(perm), wp, wn,
               _stream(stream))
     vals = gather_values(values, perm, stream) if values is not None else None
@@ -472,7 +479,7 @@ def coo_to_csr(nrow: int, rows: torch.Tensor, cols: torch.Tensor, ncol: Optional
 def gather_values(values: torch.Tensor, perm: torch.Tensor, stream=None) -> torch.Tensor:
     _need_cuda("values", values)
     _need_cuda("perm", perm, torch.int32)
-    out = torch.empty_like(values)
+    out = _output(values.shape, values.dtype, values.device)
     _lib.call("ss_gather_values", _ptr(values), int(dtype_code(values.dtype)), _ptr(perm), int(perm.numel()),
               _ptr(out), _stream(stream))
     return out
@@ -484,7 +491,7 @@ def sddmm(A: CsrMatrix, dC: torch.Tensor, B: torch.Tensor, stream=None) -> torch
     _need_cuda("B", B, A.dtype)
     if dC.shape != (A.nrow, B.shape[1]) or B.shape[0] != A.ncol:
         raise ValueError("dC must be [nrow, N] and B [ncol, N]")
-    out = torch.empty(A.nnz, dtype=torch.float32, device=dC.device)
+    out = _output(A.nnz, torch.float32, dC.device)
     d = A.descr()
     _lib.call("ss_sddmm", ctypes.byref(d), int(B.shape[1]), _ptr(dC), _ptr(B), _ptr(out), _stream(stream))
     return out

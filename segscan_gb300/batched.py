@@ -35,7 +35,7 @@ class BatchedSpMM:
         self.mats = list(mats)
         self.Bs = list(Bs)
         self.N = N
-        self.out = [torch.empty((A.nrow, N), dtype=out_dtype, device=dev) for A in mats]
+        self.out = [api._output((A.nrow, N), out_dtype, dev) for A in mats]
         count = len(mats)
         self._descr = (_lib.SsCsr * count)(*[A.descr() for A in mats])
         self._knobs = None
