@@ -290,8 +290,10 @@ def segment_workspace_size(nnz: int, N: int, strategy: str = "sr", knobs: Option
 
 def segment(src: torch.Tensor, index: torch.Tensor, dst_len: int, reduce: str = "sum",
             strategy: str = "sr", knobs: Optional[SsKnobs] = None, out: Optional[torch.Tensor] = None,
-            accumulate: bool = False, stream=None) -> torch.Tensor:
-    """dst[index[i], :] (op)= src[i, :] over a sorted index; op in sum / max / mean."""
+            accumulate: bool = False, stream=None, workspace: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """dst[index[i], :] (op)= src[i, :] over a sorted index; op in sum / max / mean.
+    workspace: a uint8 device tensor of at least segment_workspace_size()
+    + 256 bytes, else one is allocated per call."""
     if src.dim() != 2 or index.dim() != 1 or index.shape[0] != src.shape[0]:
         raise ValueError("src must be [nnz, N] and index [nnz]")
     _need_cuda("src", src)
@@ -300,7 +302,8 @@ def segment(src: torch.Tensor, index: torch.Tensor, dst_len: int, reduce: str = 
     if out is None:
         out = _output((dst_len, N), torch.float32, src.device)
     _need_cuda("out", out, torch.float32)
-    ws = _workspace(segment_workspace_size(nnz, N, strategy, knobs), src.device)
+    ws = workspace if workspace is not None else _workspace(segment_workspace_size(nnz, N, strategy, knobs),
+                                                             src.device)
     wp, wn = _aligned(ws)
     _lib.call("ss_segment_coo", int(SEG_STRATEGIES[strategy]), _ptr(src), int(dtype_code(src.dtype)),
               _ptr(index), nnz, N, int(dst_len), _ptr(out), int(REDUCES[reduce]), int(bool(accumulate)),

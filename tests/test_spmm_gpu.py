@@ -386,3 +386,33 @@ def test_concurrent_streams_and_threads(cuda):
         d64, dabs = oracle_lib.segment_coo_f64(src, A.coo_rows(), A.nrow, 0)
         check_close(seg, d64, dabs, 1e-5, None, f"thread {t} segment")
         assert "thread_per_block" in msg, msg
+
+
+def test_one_workspace_reused_across_matrices_and_calls(cuda):
+    """One caller-owned workspace, sized for the largest need, serves ebsr,
+    ebpr and segment_coo calls on different matrices back to back: the
+    arrival counts and slots are reset by each call, so nothing carries
+    over from the call before."""
+    from segscan_gb300 import api
+    mats = [synth.powerlaw(9000 + 700 * i, 8000, 2.1, 1, 1500, seed=100 + i) for i in range(3)]
+    N = 48
+    devs = [api.CsrMatrix.from_host(A, "cuda") for A in mats]
+    Bs = [torch.from_numpy(synth.dense(A.ncol, N, seed=110 + i)).cuda() for i, A in enumerate(mats)]
+    need = max(api.spmm_workspace_size(Ad, N, s) for Ad in devs for s in ("ebsr", "ebpr"))
+    need = max(need, max(api.segment_workspace_size(A.nnz, N, "sr") for A in mats))
+    ws = torch.empty(need + 256, dtype=torch.uint8, device="cuda")
+    for rep in range(2):
+        for i, (A, Ad, B) in enumerate(zip(mats, devs, Bs)):
+            C64, absC = oracle64(A, B.cpu().numpy())
+            for s in ("ebsr", "ebpr"):
+                C = torch.full((A.nrow, N), float("nan"), device="cuda")
+                api.spmm(Ad, B, s, out=C, workspace=ws)
+                torch.cuda.synchronize()
+                check_close(C.cpu().numpy(), C64, absC, 1e-5, None, f"rep {rep} matrix {i} {s}")
+            idx = torch.from_numpy(A.coo_rows()).cuda()
+            src = torch.from_numpy(synth.dense(A.nnz, N, seed=120 + i)).cuda()
+            out = torch.full((A.nrow, N), float("nan"), device="cuda")
+            api.segment(src, idx, A.nrow, "sum", "sr", out=out, workspace=ws)
+            torch.cuda.synchronize()
+            d64, dabs = oracle_lib.segment_coo_f64(src.cpu().numpy(), A.coo_rows(), A.nrow, 0)
+            check_close(out.cpu().numpy(), d64, dabs, 1e-5, None, f"rep {rep} matrix {i} segment")
