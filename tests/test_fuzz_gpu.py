@@ -162,3 +162,33 @@ def test_batched_fuzz(cuda, seed):
         C64, absC = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B)
         check_close(plan.out[i].cpu().numpy(), C64, absC, 1e-5, None,
                     f"seed {seed}: matrix {i} of {count} ({A.nrow}x{A.ncol}, nnz {A.nnz}) N={N} target={target}")
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_coo_to_csr_fuzz(cuda, seed):
+    """Random COO (shuffled, skewed, some rows out of range) to CSR, bit for
+    bit against a stable argsort by row."""
+    rng = np.random.default_rng(15000 + seed)
+    nrow = int(rng.integers(1, 40000))
+    nnz = int(rng.integers(0, 300000))
+    rows = rng.integers(0, nrow, size=nnz).astype(np.int32)
+    if nnz and rng.random() < 0.5:  # one heavy row
+        rows[rng.random(nnz) < rng.uniform(0.05, 0.6)] = int(rng.integers(0, nrow))
+    if nnz and rng.random() < 0.3:  # entries outside [0, nrow) are left out
+        bad = rng.random(nnz) < 0.02
+        rows[bad] = np.where(rng.random(int(bad.sum())) < 0.5, -1, nrow + 5)
+    ncol = int(rng.integers(1, 50000))
+    cols = rng.integers(0, ncol, size=nnz).astype(np.int32)
+    vals = rng.standard_normal(nnz).astype(np.float32)
+    A, perm = api.coo_to_csr(nrow, torch.from_numpy(rows).cuda(), torch.from_numpy(cols).cuda(), ncol=ncol,
+                             values=torch.from_numpy(vals).cuda())
+    torch.cuda.synchronize()
+    valid = (rows >= 0) & (rows < nrow)
+    order = np.nonzero(valid)[0][np.argsort(rows[valid], kind="stable")].astype(np.int32)
+    indptr = np.concatenate([[0], np.cumsum(np.bincount(rows[valid], minlength=nrow))]).astype(np.int32)
+    m = int(valid.sum())
+    what = f"seed {seed}: nrow={nrow} nnz={nnz} valid={m}"
+    assert np.array_equal(A.indptr.cpu().numpy(), indptr), what
+    assert np.array_equal(perm.cpu().numpy()[:m], order), what
+    assert np.array_equal(A.indices.cpu().numpy()[:m], cols[order]), what
+    assert np.array_equal(A.values.cpu().numpy()[:m], vals[order]), what
