@@ -14,9 +14,11 @@
 //   * errors throw segscan_gb300::Error (the reference calls exit());
 //   * an optional trailing cudaStream_t (the reference uses the legacy
 //     default stream);
-//   * scratch for the element-balanced strategies comes from a per-device
-//     workspace this header grows with cudaMalloc on first use, outside the
-//     hot path; C callers pass their own through the C ABI instead.
+//   * scratch for the element-balanced strategies comes from a workspace
+//     per (device, stream) that this header grows with cudaMalloc on first
+//     use, outside the hot path: calls on one stream run in order and can
+//     share it, calls on different streams never do; C callers pass their
+//     own through the C ABI instead.
 // The ebpr / rbpr / ebsr launchers ADD into C (the reference's callers zero
 // C first, test-cg/include/util/check.cuh:71), rbsr overwrites C, and the
 // segment_coo launchers ADD into dst, as in the reference.
@@ -26,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -74,18 +77,24 @@ template <class Index, class DType> struct SpMatCsrDescr_t {
   }
 };
 
-// Per-device scratch, grown on demand and kept for the life of the process.
+// Scratch per (device, stream), grown on demand and kept for the life of
+// the process.  Work on one stream is ordered, so its calls share a buffer;
+// a buffer is only replaced (to grow it) after its stream has drained.
 class Workspace {
  public:
-  static void *get(size_t bytes) {
+  static void *get(size_t bytes, cudaStream_t stream) {
     static std::mutex mu;
-    static std::vector<std::pair<void *, size_t>> per_dev(64, {nullptr, 0});
+    static std::map<std::pair<int, cudaStream_t>, std::pair<void *, size_t>> slots;
     int dev = 0;
     check(cudaGetDevice(&dev) == cudaSuccess ? SS_OK : SS_ERR_CUDA, "cudaGetDevice");
     std::lock_guard<std::mutex> lock(mu);
-    auto &slot = per_dev.at(dev);
+    auto &slot = slots[{dev, stream}];
     if (slot.second < bytes) {
-      if (slot.first) cudaFree(slot.first);
+      if (slot.first) {
+        // earlier calls on this stream may still read the old buffer
+        if (cudaStreamSynchronize(stream) != cudaSuccess) throw Error(SS_ERR_CUDA, "workspace stream sync failed");
+        cudaFree(slot.first);
+      }
       slot = {nullptr, 0};
       if (cudaMalloc(&slot.first, bytes) != cudaSuccess) throw Error(SS_ERR_CUDA, "workspace cudaMalloc failed");
       slot.second = bytes;
@@ -115,7 +124,7 @@ inline void spmm(int strategy, const SpMatCsrDescr_t<Index, DType> &A, int N, co
   ss_csr d = A.descr();
   size_t ws = 0;
   check(ss_spmm_workspace_size(strategy, &d, N, &k, &ws), where);
-  void *w = ws ? Workspace::get(ws) : nullptr;
+  void *w = ws ? Workspace::get(ws, s) : nullptr;
   check(ss_spmm(strategy, &d, N, B, C, dtype_of<DType>::value, accumulate, &k, w, ws, (void *)s), where);
 }
 
@@ -125,7 +134,7 @@ inline void segment(int strategy, const V *src, const I *index, int nnz, int N, 
   static_assert(std::is_same<V, float>::value, "segment_coo dst is float");
   size_t ws = 0;
   check(ss_segment_coo_workspace_size(strategy, nnz, N, &k, &ws), where);
-  void *w = ws ? Workspace::get(ws) : nullptr;
+  void *w = ws ? Workspace::get(ws, s) : nullptr;
   check(ss_segment_coo(strategy, src, dtype_of<V>::value, reinterpret_cast<const int32_t *>(index), nnz, N, dst_len,
                        dst, SS_SUM, 1, &k, w, ws, (void *)s),
         where);

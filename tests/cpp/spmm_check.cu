@@ -132,6 +132,33 @@ int main() {
       cudaFree(d_src);
       cudaFree(d_index);
     }
+    // two streams at once: each gets its own workspace from the header, so
+    // interleaved ebsr / ebpr calls on them do not share scratch
+    {
+      cudaStream_t s1, s2;
+      cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking);
+      cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+      DType *d_C2;
+      cudaMalloc(&d_C2, sizeof(DType) * M * N);
+      std::vector<float> got2((size_t)M * N);
+      for (int rep = 0; rep < 8; rep++) {
+        cudaMemsetAsync(d_C, 0, sizeof(DType) * M * N, s1);
+        cudaMemsetAsync(d_C2, 0, sizeof(DType) * M * N, s2);
+        csrspmm_rowcaching_nnzbalance_cg<Index, DType, 4, 256, 4, 1, 1, 16>(H, N, d_B, d_C, s1);
+        csrspmm_parreduce_nnzbalance_cg<Index, DType, 5, 256, 5, 1, 8>(H, N, d_B, d_C2, s2);
+      }
+      cudaStreamSynchronize(s1);
+      cudaStreamSynchronize(s2);
+      cudaMemcpy(got.data(), d_C, sizeof(DType) * M * N, cudaMemcpyDeviceToHost);
+      cudaMemcpy(got2.data(), d_C2, sizeof(DType) * M * N, cudaMemcpyDeviceToHost);
+      snprintf(name, sizeof(name), "N=%d ebsr on stream 1", N);
+      check_result(name, M, N, got, ref, absref);
+      snprintf(name, sizeof(name), "N=%d ebpr on stream 2", N);
+      check_result(name, M, N, got2, ref, absref);
+      cudaFree(d_C2);
+      cudaStreamDestroy(s1);
+      cudaStreamDestroy(s2);
+    }
     cudaFree(d_indptr); cudaFree(d_indices); cudaFree(d_data); cudaFree(d_B); cudaFree(d_C);
   }
   printf("%s\n", failures ? "FAILED" : "ALL PASSED");
