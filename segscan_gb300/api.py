@@ -212,8 +212,13 @@ class SpmmPlan(_Plan):
 
     def __init__(self, A: CsrMatrix, N: int, strategy: str = "ebsr", knobs: Optional[SsKnobs] = None,
                  out_dtype: torch.dtype = torch.float32, accumulate: bool = False, stream=None):
+        """strategy="auto" takes the autotuner's strategy and knobs for A at
+        width N (measured once per shape signature, then cached)."""
         self.A = A
         self.N = int(N)
+        if strategy == "auto":
+            from . import autotune
+            strategy, knobs = autotune.best(A, self.N)
         self.strategy = strategy
         self.knobs = knobs if knobs is not None else default_knobs(strategy, self.N)
         self.out_dtype = out_dtype

@@ -338,6 +338,21 @@ def test_plan_run_and_graph_match_spmm(cuda, strategy):
         plan.run(B.to(torch.bfloat16), out)
 
 
+def test_plan_auto_strategy(cuda):
+    """SpmmPlan(strategy="auto") runs the autotuner's pick, within 1e-5 of FP64."""
+    from segscan_gb300 import api
+    A = synth.powerlaw(20000, 20000, 2.1, 1, 2000, seed=7)
+    Ad = api.CsrMatrix.from_host(A, "cuda")
+    B = synth.dense(A.ncol, 16, seed=8)
+    plan = api.SpmmPlan(Ad, 16, "auto")
+    assert plan.strategy in ("ebpr", "rbpr", "ebsr", "rbsr")
+    out = torch.full((A.nrow, 16), float("nan"), device="cuda")
+    plan.run(torch.from_numpy(B).cuda(), out)
+    torch.cuda.synchronize()
+    C64, absC = oracle64(A, B)
+    check_close(out.cpu().numpy(), C64, absC, 1e-5, None, f"auto plan ({plan.strategy})")
+
+
 def test_concurrent_streams_and_threads(cuda):
     """The C ABI is stream-ordered and reentrant: four host threads, each
     with its own stream, matrix and workspace, call SpMM and segment_coo
