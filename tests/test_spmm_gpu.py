@@ -388,12 +388,53 @@ def test_concurrent_streams_and_threads(cuda):
         except Exception as exc:  # surfaced in the main thread
             errors.append(exc)
 
+    # two more threads at the same time: the narrow walk at N = 4 and the
+    # device transpose, each on its own stream
+    extra = {}
+
+    def narrow():
+        try:
+            A = synth.powerlaw(30000, 30000, 2.1, 1, 3000, seed=64)
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                Ad = api.CsrMatrix.from_host(A, "cuda")
+                B = torch.from_numpy(synth.dense(A.ncol, 4, seed=65)).cuda()
+                k = api.make_knobs("ebsr", 4, group_factor=0, coarsen_factor=4, thread_nz=64, block_denom=1)
+                for _ in range(20):
+                    C = api.spmm(Ad, B, "ebsr", knobs=k, stream=s)
+                s.synchronize()
+                extra["narrow"] = (A, B.cpu().numpy(), C.cpu().numpy())
+        except Exception as exc:
+            errors.append(exc)
+
+    def transpose():
+        try:
+            A = synth.powerlaw(25000, 18000, 2.1, 1, 3000, seed=66)
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                Ad = api.CsrMatrix.from_host(A, "cuda")
+                for _ in range(10):
+                    AT, perm = api.transpose(Ad, stream=s)
+                s.synchronize()
+                extra["transpose"] = (A, AT.indptr.cpu().numpy(), AT.indices.cpu().numpy(), perm.cpu().numpy())
+        except Exception as exc:
+            errors.append(exc)
+
     threads = [threading.Thread(target=work, args=(t,)) for t in range(4)]
+    threads += [threading.Thread(target=narrow), threading.Thread(target=transpose)]
     for th in threads:
         th.start()
     for th in threads:
         th.join()
     assert not errors, errors
+    A, B, C = extra["narrow"]
+    C64, absC = oracle64(A, B)
+    check_close(C, C64, absC, 1e-5, None, "narrow walk thread")
+    A, t_indptr, t_indices, perm = extra["transpose"]
+    order = np.argsort(A.indices, kind="stable")
+    assert np.array_equal(perm, order.astype(np.int32))
+    assert np.array_equal(t_indices, np.repeat(np.arange(A.nrow, dtype=np.int32), np.diff(A.indptr))[order])
+    assert np.array_equal(t_indptr, np.concatenate([[0], np.cumsum(np.bincount(A.indices, minlength=A.ncol))]))
     for t, (A, B, strategy) in enumerate(jobs):
         C, seg, src, msg = results[t]
         C64, absC = oracle64(A, B)
