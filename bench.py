@@ -517,14 +517,19 @@ def run_ours(args):
         t = float(tt.item())
 
     # end to end through the public API: host inputs in pinned memory,
-    # H2D of A and B, the SpMM, D2H of C, every step; consecutive steps
-    # alternate between two streams and buffer sets, so one step's copies
-    # overlap the next step's (each step still moves all of its own bytes)
+    # H2D of A and B, the SpMM, D2H of C, every step.  Copies in, the SpMM
+    # and the copy out run on three streams, and consecutive steps alternate
+    # between two device buffer sets, ordered by events: step i's inputs go
+    # up while step i-1 computes and step i-2's C comes down, so both link
+    # directions stay busy (each step still moves all of its own bytes)
     h_indptr = torch.from_numpy(A.indptr).pin_memory()
     h_indices = torch.from_numpy(A.indices).pin_memory()
     h_values = torch.from_numpy(A.values).pin_memory()
     h_B = torch.from_numpy(B).pin_memory()
-    e2e_streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    e2e_streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)]  # in, compute, out
+    ev_in = [torch.cuda.Event() for _ in range(2)]     # set k's inputs are on the device
+    ev_done = [torch.cuda.Event() for _ in range(2)]   # set k's SpMM finished (its inputs are free)
+    ev_out = [torch.cuda.Event() for _ in range(2)]    # set k's C is on the host (its C is free)
     sets = []
     for _ in range(2):
         d = dict(indptr=torch.empty_like(Ad.indptr), indices=torch.empty_like(Ad.indices),
@@ -537,15 +542,27 @@ def run_ours(args):
     d2h = sets[0]["hC"].numel() * sets[0]["hC"].element_size()
 
     def e2e_step(i):
-        s_ = e2e_streams[i % 2]
-        d = sets[i % 2]
-        with torch.cuda.stream(s_):
+        k = i % 2
+        d = sets[k]
+        s_in, s_cmp, s_out = e2e_streams
+        with torch.cuda.stream(s_in):
+            if i >= 2:
+                s_in.wait_event(ev_done[k])  # the SpMM of step i-2 no longer reads set k's inputs
             d["indptr"].copy_(h_indptr, non_blocking=True)
             d["indices"].copy_(h_indices, non_blocking=True)
             d["values"].copy_(h_values, non_blocking=True)
             d["B"].copy_(h_B, non_blocking=True)
-            api.spmm(d["A"], d["B"], strategy, knobs=knobs, out=d["C"], workspace=d["ws"], stream=s_)
+            ev_in[k].record(s_in)
+        with torch.cuda.stream(s_cmp):
+            s_cmp.wait_event(ev_in[k])
+            if i >= 2:
+                s_cmp.wait_event(ev_out[k])  # step i-2's C has left set k
+            api.spmm(d["A"], d["B"], strategy, knobs=knobs, out=d["C"], workspace=d["ws"], stream=s_cmp)
+            ev_done[k].record(s_cmp)
+        with torch.cuda.stream(s_out):
+            s_out.wait_event(ev_done[k])
             d["hC"].copy_(d["C"], non_blocking=True)
+            ev_out[k].record(s_out)
 
     def e2e_run(k):
         for s_ in e2e_streams:
