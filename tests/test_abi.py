@@ -104,3 +104,26 @@ def test_bad_arguments_rejected_without_launch(lib):
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "nope.so")
+
+
+def test_python_api_refuses_host_tensors_and_bad_shapes(lib):
+    """The Python entry points check their arguments before any launch: host
+    tensors, mismatched shapes and unknown strategies are refused on a
+    machine without a GPU as on one with it."""
+    import torch
+    from segscan_gb300 import api
+    indptr = torch.tensor([0, 1, 2], dtype=torch.int32)
+    indices = torch.tensor([0, 1], dtype=torch.int32)
+    A = api.CsrMatrix(2, 2, indptr, indices, torch.ones(2))
+    with pytest.raises(ValueError, match="CUDA"):
+        A.descr()
+    with pytest.raises(ValueError, match="B must be"):
+        api.spmm(A, torch.ones(3, 4), "ebsr")
+    with pytest.raises(ValueError, match="CUDA"):
+        api.spmm(A, torch.ones(2, 4), "ebsr")
+    with pytest.raises(ValueError, match="src must be"):
+        api.segment(torch.ones(3, 4), torch.zeros(2, dtype=torch.int32), 2)
+    with pytest.raises(KeyError):
+        api.default_knobs("csr_magic", 4)
+    with pytest.raises(TypeError, match="unknown knob"):
+        api.make_knobs("ebsr", 4, warp_count=2)
