@@ -101,6 +101,25 @@ def test_bad_arguments_rejected_without_launch(lib):
         (Status.WORKSPACE, Status.CUDA)
 
 
+@pytest.mark.parametrize("N", [1, 3, 4, 8, 16, 33, 64, 128, 130])
+def test_autotuner_candidates_pass_knob_validation(lib, N):
+    """Every tuple the autotuner may time, and its no-measurement pick, is a
+    tuple the library accepts (so tuning never spends a trial on a refused
+    launch), for FP32 and 16-bit storage at widths of every residue."""
+    import torch
+    from segscan_gb300 import api, autotune
+    n = ctypes.c_size_t()
+    features = {"cv": 3.0, "max": 20000}, {"cv": 0.2, "max": 30}
+    for code, dtype in ((0, torch.float32), (1, torch.bfloat16), (2, torch.float16)):
+        A = SsCsr(1000, 1000, 5000, 256, 512, 1024, code)
+        picks = autotune.candidates(N, dtype) + [autotune.heuristic(f, N, dtype) for f in features]
+        for strategy, kw in picks:
+            k = api.make_knobs(strategy, N, **kw)
+            st = lib.ss_spmm_workspace_size(int(api.STRATEGIES[strategy]), ctypes.byref(A), N, ctypes.byref(k),
+                                            ctypes.byref(n))
+            assert st == Status.OK, (strategy, kw, dtype, lib.ss_last_error())
+
+
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "nope.so")
