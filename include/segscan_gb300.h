@@ -281,7 +281,9 @@ ss_status ss_index_validate(const int32_t *index, int nnz, int dst_len,
  * build stopping after the file's declared entry count (an expanded
  * symmetric file loses its last rows' entries there); SS_MTX_FULL keeps every
  * entry and also expands skew-symmetric and hermitian files.  Errors are
- * status codes (the reference exit()s).  ss_mtx_shape then ss_mtx_csr copy
+ * status codes (the reference exit()s): SS_ERR_BAD_DATA for a malformed file,
+ * SS_ERR_CAPACITY when host memory runs out or a full-mode expansion passes
+ * 2^31 - 1 entries.  ss_mtx_shape then ss_mtx_csr copy
  * the result into caller buffers of nrow + 1 and nnz int32. */
 typedef struct ss_mtx ss_mtx;
 enum { SS_MTX_REFERENCE = 0, SS_MTX_FULL = 1 };

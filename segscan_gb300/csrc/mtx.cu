@@ -19,6 +19,8 @@
 #include <cctype>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -77,17 +79,10 @@ std::string lower(std::string s) {
   return s;
 }
 
-}  // namespace
-}  // namespace ss
-
-using namespace ss;
-
-extern "C" {
-
-ss_status ss_mtx_read(const char *path, int mode, ss_mtx **out) {
-  if (!path || !out) return fail(SS_ERR_INVALID_ARG, "null path or output");
-  if (mode != SS_MTX_REFERENCE && mode != SS_MTX_FULL) return fail(SS_ERR_INVALID_ARG, "mode %d unknown", mode);
-  *out = nullptr;
+// The body of ss_mtx_read.  Host allocations may throw std::bad_alloc; the
+// entry point turns that into a status, since no exception may cross the C
+// boundary.
+ss_status mtx_read(const char *path, int mode, ss_mtx **out) {
   FILE *f = fopen(path, "rb");
   if (!f) return fail(SS_ERR_INVALID_ARG, "cannot open %s", path);
   std::vector<char> buf;
@@ -129,8 +124,14 @@ ss_status ss_mtx_read(const char *path, int mode, ss_mtx **out) {
       K > 0x7fffffff || Z > 0x7fffffff)
     return fail(SS_ERR_BAD_DATA, "%s: bad size line", path);
 
+  // Each entry takes at least three bytes of text ("i j" and a separator,
+  // the last one possibly without), so a file holds at most size / 3 + 1 of
+  // them whatever its size line declares: reserve no more than that, so a
+  // short file with a huge declared count fails on its missing entries
+  // instead of on a huge allocation.
   std::vector<int32_t> rows, cols;
-  const size_t cap = (size_t)Z * (expand ? 2 : 1);
+  const size_t fit = std::min((size_t)Z, buf.size() / 3 + 1);
+  const size_t cap = fit * (expand ? 2 : 1);
   rows.reserve(cap);
   cols.reserve(cap);
   for (long long e = 0; e < Z; e++) {
@@ -160,7 +161,7 @@ ss_status ss_mtx_read(const char *path, int mode, ss_mtx **out) {
     std::vector<int64_t> cur(start.begin(), start.end() - 1);
     for (size_t e = 0; e < n; e++) sorted[(size_t)cur[(size_t)rows[e]]++] = cols[e];
   }
-  ss_mtx *m = new ss_mtx;
+  std::unique_ptr<ss_mtx> m(new ss_mtx);
   m->nrow = (int)M;
   m->ncol = (int)K;
   m->indptr.assign((size_t)M + 1, 0);
@@ -173,10 +174,32 @@ ss_status ss_mtx_read(const char *path, int mode, ss_mtx **out) {
     std::sort(a, b);
     if (expand) b = std::unique(a, b);
     for (int32_t *q = a; q < b && m->indices.size() < limit; q++) m->indices.push_back(*q);
+    // int32 row pointers: a symmetric expansion (full mode) can double the
+    // declared count past them
+    if (m->indices.size() > (size_t)0x7fffffff)
+      return fail(SS_ERR_CAPACITY, "%s: more than 2^31 - 1 entries after symmetric expansion", path);
     m->indptr[(size_t)i + 1] = (int32_t)m->indices.size();
   }
-  *out = m;
+  *out = m.release();
   return SS_OK;
+}
+
+}  // namespace
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" {
+
+ss_status ss_mtx_read(const char *path, int mode, ss_mtx **out) {
+  if (!path || !out) return fail(SS_ERR_INVALID_ARG, "null path or output");
+  if (mode != SS_MTX_REFERENCE && mode != SS_MTX_FULL) return fail(SS_ERR_INVALID_ARG, "mode %d unknown", mode);
+  *out = nullptr;
+  try {
+    return mtx_read(path, mode, out);
+  } catch (const std::bad_alloc &) {
+    return fail(SS_ERR_CAPACITY, "%s: out of host memory while reading", path);
+  }
 }
 
 ss_status ss_mtx_shape(const ss_mtx *m, int *nrow, int *ncol, int *nnz) {

@@ -90,6 +90,36 @@ def test_malformed_files_refused(lib, tmp_path, body, status):
     assert e.value.status == status
 
 
+_CAPPED_READ = r"""
+import ctypes, resource, sys
+resource.setrlimit(resource.RLIMIT_AS, (2 << 30, 2 << 30))
+lib = ctypes.CDLL(sys.argv[1])
+h = ctypes.c_void_p()
+print(*(lib.ss_mtx_read(sys.argv[2].encode(), mode, ctypes.byref(h)) for mode in (0, 1)))
+"""
+
+
+@pytest.mark.parametrize("size_line, status", [
+    ("3 3 2100000000", Status.BAD_DATA),   # declared count far beyond what the file holds
+    ("2147483647 2147483647 1", Status.CAPACITY),  # row pointers beyond the host memory allowed
+])
+def test_huge_declared_sizes_return_a_status(lib, tmp_path, size_line, status):
+    """A short file whose size line declares a huge matrix gets a status code
+    in both modes, in a process limited to 2 GB of address space: no
+    reservation sized by the declared count alone, and an allocation failure
+    is reported instead of ending the process (no exception crosses the C
+    boundary)."""
+    import subprocess
+    import sys
+    from segscan_gb300 import _lib
+    p = tmp_path / "huge.mtx"
+    p.write_text(f"%%MatrixMarket matrix coordinate pattern symmetric\n{size_line}\n1 2\n")
+    r = subprocess.run([sys.executable, "-c", _CAPPED_READ, str(_lib.LIB_PATH), str(p)], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-500:]
+    assert r.stdout.split() == [str(int(status))] * 2
+
+
 def test_missing_file(lib, tmp_path):
     with pytest.raises(SegscanError) as e:
         mtx.read(tmp_path / "absent.mtx")
