@@ -14,8 +14,11 @@ is a call into libsegscan_gb300.so.  Nothing here falls back to PyTorch.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import dataclasses
+import functools
+import inspect
 from typing import Optional
 
 import numpy as np
@@ -47,6 +50,41 @@ def _stream(stream) -> int:
     if stream is None:
         stream = torch.cuda.current_stream()
     return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+def _on(stream):
+    """Context in which the launch stream is the current stream (nothing to
+    do when the caller passed none, so the current stream is the launch
+    stream already)."""
+    if stream is None:
+        return contextlib.nullcontext()
+    if not isinstance(stream, torch.cuda.Stream):
+        handle = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        if handle == torch.cuda.current_stream().cuda_stream:
+            return contextlib.nullcontext()
+        stream = torch.cuda.ExternalStream(handle)
+    return torch.cuda.stream(stream)
+
+
+def _allocates_on_launch_stream(fn):
+    """Runs fn with its ``stream`` argument as the current stream.
+
+    torch's caching allocator ties each block to the stream current when it
+    was allocated and, once the block is freed, hands it out again in that
+    stream's order only.  A call that allocated its workspace and outputs on
+    the current stream but launched on another could otherwise have its
+    freed workspace handed out while the kernel still uses it, or write an
+    output block that earlier work on the current stream still reads.
+    Allocating on the launch stream, as torch's own operators do, closes
+    both."""
+    pos = list(inspect.signature(fn).parameters).index("stream")
+
+    @functools.wraps(fn)
+    def wrapper(*args, **kw):
+        stream = kw.get("stream", args[pos] if len(args) > pos else None)
+        with _on(stream):
+            return fn(*args, **kw)
+    return wrapper
 
 
 def _need_cuda(name: str, t: torch.Tensor, dtype: Optional[torch.dtype] = None) -> None:
@@ -145,6 +183,7 @@ def spmm_workspace_size(A: CsrMatrix, N: int, strategy: str, knobs: Optional[SsK
     return int(n.value)
 
 
+@_allocates_on_launch_stream
 def spmm(A: CsrMatrix, B: torch.Tensor, strategy: str = "ebsr", knobs: Optional[SsKnobs] = None,
          out: Optional[torch.Tensor] = None, accumulate: bool = False,
          out_dtype: Optional[torch.dtype] = None, workspace: Optional[torch.Tensor] = None,
@@ -210,6 +249,7 @@ class SpmmPlan(_Plan):
     6-12 us.  The plan keeps A's tensors and its workspace alive; the caller
     keeps B and out alive across replays of a captured graph."""
 
+    @_allocates_on_launch_stream
     def __init__(self, A: CsrMatrix, N: int, strategy: str = "ebsr", knobs: Optional[SsKnobs] = None,
                  out_dtype: torch.dtype = torch.float32, accumulate: bool = False, stream=None):
         """strategy="auto" takes the autotuner's strategy and knobs for A at
@@ -253,6 +293,7 @@ class SegmentPlan(_Plan):
     records it into a CUDA graph, as for SpmmPlan.  The plan keeps the
     index and its workspace alive."""
 
+    @_allocates_on_launch_stream
     def __init__(self, index: torch.Tensor, dst_len: int, N: int, reduce: str = "sum", strategy: str = "sr",
                  src_dtype: torch.dtype = torch.float32, knobs: Optional[SsKnobs] = None, accumulate: bool = False,
                  stream=None):
@@ -293,6 +334,7 @@ def segment_workspace_size(nnz: int, N: int, strategy: str = "sr", knobs: Option
     return int(n.value)
 
 
+@_allocates_on_launch_stream
 def segment(src: torch.Tensor, index: torch.Tensor, dst_len: int, reduce: str = "sum",
             strategy: str = "sr", knobs: Optional[SsKnobs] = None, out: Optional[torch.Tensor] = None,
             accumulate: bool = False, stream=None, workspace: Optional[torch.Tensor] = None) -> torch.Tensor:
@@ -316,6 +358,7 @@ def segment(src: torch.Tensor, index: torch.Tensor, dst_len: int, reduce: str = 
     return out
 
 
+@_allocates_on_launch_stream
 def row_ids(indptr: torch.Tensor, nnz: int, elems: Optional[torch.Tensor] = None, stream=None) -> torch.Tensor:
     """Row of each nonzero (binary_search_segment_number, check.cuh:88-102)."""
     _need_cuda("indptr", indptr, torch.int32)
@@ -328,6 +371,7 @@ def row_ids(indptr: torch.Tensor, nnz: int, elems: Optional[torch.Tensor] = None
     return rows
 
 
+@_allocates_on_launch_stream
 def validate(A: CsrMatrix, stream=None) -> int:
     """0 when A is well formed, else the flag bits of ss_csr_validate (synchronises)."""
     flag = torch.zeros(1, dtype=torch.int32, device=A.indptr.device)
@@ -336,6 +380,7 @@ def validate(A: CsrMatrix, stream=None) -> int:
     return int(flag.item())
 
 
+@_allocates_on_launch_stream
 def validate_index(index: torch.Tensor, dst_len: int, stream=None) -> int:
     flag = torch.zeros(1, dtype=torch.int32, device=index.device)
     _lib.call("ss_index_validate", _ptr(index), int(index.numel()), int(dst_len), _ptr(flag), _stream(stream))
@@ -439,6 +484,7 @@ def segment_coo_sorted_sr(src, index, nnz, N, dst, *, CoarsenFactor, ThreadNz, D
 # ---------------------------------------------------------------------------
 # Transpose, value gather, SDDMM (backward pass building blocks)
 # ---------------------------------------------------------------------------
+@_allocates_on_launch_stream
 def transpose(A: CsrMatrix, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
     """(A^T pattern with values gathered, perm): stable counting-sort transpose
     on the device (dataloader.hpp:109-144); perm[q] = source nonzero of entry q."""
@@ -459,6 +505,7 @@ def transpose(A: CsrMatrix, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
     return CsrMatrix(A.ncol, A.nrow, t_indptr, t_indices, vals), perm
 
 
+@_allocates_on_launch_stream
 def coo_to_csr(nrow: int, rows: torch.Tensor, cols: torch.Tensor, ncol: Optional[int] = None,
                values: Optional[torch.Tensor] = None, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
     """(CSR matrix, perm) from COO rows/cols on the device: a stable counting
@@ -484,6 +531,7 @@ def coo_to_csr(nrow: int, rows: torch.Tensor, cols: torch.Tensor, ncol: Optional
     return CsrMatrix(nrow, K, indptr, out_cols, vals), perm
 
 
+@_allocates_on_launch_stream
 def gather_values(values: torch.Tensor, perm: torch.Tensor, stream=None) -> torch.Tensor:
     _need_cuda("values", values)
     _need_cuda("perm", perm, torch.int32)
@@ -493,6 +541,7 @@ def gather_values(values: torch.Tensor, perm: torch.Tensor, stream=None) -> torc
     return out
 
 
+@_allocates_on_launch_stream
 def sddmm(A: CsrMatrix, dC: torch.Tensor, B: torch.Tensor, stream=None) -> torch.Tensor:
     """dvals[p] = dot(dC[i, :], B[k, :]) at every stored nonzero p = (i, k); FP32."""
     _need_cuda("dC", dC, torch.float32)

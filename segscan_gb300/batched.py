@@ -21,6 +21,7 @@ from ._lib import SsKnobs
 class BatchedSpMM:
     """C[m] = A[m] @ B[m] for every m, one persistent launch per step."""
 
+    @api._allocates_on_launch_stream
     def __init__(self, mats: Sequence[api.CsrMatrix], Bs: Sequence[torch.Tensor],
                  out_dtype: torch.dtype = torch.float32, knobs: Optional[Sequence[SsKnobs]] = None,
                  stream=None):

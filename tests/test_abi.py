@@ -120,6 +120,23 @@ def test_autotuner_candidates_pass_knob_validation(lib, N):
             assert st == Status.OK, (strategy, kw, dtype, lib.ss_last_error())
 
 
+def test_launch_stream_argument_found_by_position_and_keyword(monkeypatch):
+    """The Python calls make their stream argument current while they
+    allocate and launch; the wrapper finds it passed by keyword, by
+    position, or not at all."""
+    import contextlib
+    from segscan_gb300 import api
+    seen = []
+    monkeypatch.setattr(api, "_on", lambda s: (seen.append(s), contextlib.nullcontext())[1])
+
+    @api._allocates_on_launch_stream
+    def call(a, b=None, stream=None):
+        return a
+
+    assert call(1) == 1 and call(1, 2, "s1") == 1 and call(1, stream="s2") == 1
+    assert seen == [None, "s1", "s2"]
+
+
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "nope.so")

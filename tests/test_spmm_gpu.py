@@ -472,3 +472,36 @@ def test_one_workspace_reused_across_matrices_and_calls(cuda):
             torch.cuda.synchronize()
             d64, dabs = oracle_lib.segment_coo_f64(src.cpu().numpy(), A.coo_rows(), A.nrow, 0)
             check_close(out.cpu().numpy(), d64, dabs, 1e-5, None, f"rep {rep} matrix {i} segment")
+
+
+def test_stream_argument_without_entering_the_stream(cuda):
+    """spmm and segment given stream=s while another stream is current
+    allocate their workspace and outputs on s.  Memory allocated and
+    overwritten on the current stream right after each call therefore never
+    lands on a block the launch on s still uses; every result matches
+    FP64."""
+    from segscan_gb300 import api
+    A = synth.powerlaw(60000, 60000, 2.1, 1, 6000, seed=130)
+    N = 64
+    B = synth.dense(A.ncol, N, seed=131)
+    Ad = api.CsrMatrix.from_host(A, "cuda")
+    Bd = torch.from_numpy(B).cuda()
+    idx = torch.from_numpy(A.coo_rows()).cuda()
+    src_h = synth.dense(A.nnz, 16, seed=132)
+    src = torch.from_numpy(src_h).cuda()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    outs = []
+    for strategy in ("ebsr", "ebpr", "ebsr"):
+        C = api.spmm(Ad, Bd, strategy, stream=s)
+        seg = api.segment(src, idx, A.nrow, "sum", stream=s)
+        junk = torch.empty(64 << 20, dtype=torch.uint8, device="cuda").fill_(0xFF)  # on the current stream
+        del junk
+        outs.append((strategy, C, seg))
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    C64, absC = oracle64(A, B)
+    d64, dabs = oracle_lib.segment_coo_f64(src_h, A.coo_rows(), A.nrow, 0)
+    for i, (strategy, C, seg) in enumerate(outs):
+        check_close(C.cpu().numpy(), C64, absC, 1e-5, None, f"call {i} {strategy} on a side stream")
+        check_close(seg.cpu().numpy(), d64, dabs, 1e-5, None, f"call {i} segment on a side stream")
