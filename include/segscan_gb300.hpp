@@ -80,6 +80,9 @@ template <class Index, class DType> struct SpMatCsrDescr_t {
 // Scratch per (device, stream), grown on demand and kept for the life of
 // the process.  Work on one stream is ordered, so its calls share a buffer;
 // a buffer is only replaced (to grow it) after its stream has drained.
+// Host threads that launch on one shared stream must serialise their calls:
+// a growth on one thread between another thread's get() and its launch
+// would free the buffer that launch was given.
 class Workspace {
  public:
   static void *get(size_t bytes, cudaStream_t stream) {
