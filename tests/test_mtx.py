@@ -120,6 +120,43 @@ def test_huge_declared_sizes_return_a_status(lib, tmp_path, size_line, status):
     assert r.stdout.split() == [str(int(status))] * 2
 
 
+def test_mutated_files_parse_or_are_refused(lib, tmp_path):
+    """Seeded byte-level mutations of the committed files (deletions,
+    insertions of banner and digit characters, random bytes, truncation):
+    each read either gives a well-formed CSR (row pointers from 0 to nnz,
+    non-decreasing, columns inside the matrix) or is refused with
+    SS_ERR_BAD_DATA, in both modes."""
+    import random
+    bases = [p.read_bytes() for p in sorted(GOLD.glob("mtx_*.mtx"))]
+    alphabet = b"0123456789 \t\r\n%-+.eE%%MatrixMarketcoordinatepatternsymmetricgeneralrealinteger"
+    rng = random.Random(7)
+    p = tmp_path / "mutated.mtx"
+    parsed = 0
+    for _ in range(400):
+        b = bytearray(rng.choice(bases))
+        for _ in range(rng.randint(1, 8)):
+            op, pos = rng.random(), rng.randint(0, len(b))
+            if op < 0.3 and b:
+                del b[pos:pos + rng.randint(1, 12)]
+            elif op < 0.6:
+                b[pos:pos] = bytes(rng.choice(alphabet) for _ in range(rng.randint(1, 12)))
+            elif op < 0.8 and b:
+                b[min(pos, len(b) - 1)] = rng.randrange(256)
+            else:
+                del b[pos:]
+        p.write_bytes(bytes(b))
+        for mode in ("reference", "full"):
+            try:
+                A = mtx.read(p, mode)
+            except SegscanError as e:
+                assert e.status == Status.BAD_DATA, str(e)
+                continue
+            parsed += 1
+            assert A.indptr[0] == 0 and A.indptr[-1] == A.nnz and np.all(np.diff(A.indptr) >= 0)
+            assert A.indices.size == A.nnz and np.all((A.indices >= 0) & (A.indices < max(A.ncol, 1)))
+    assert parsed > 0
+
+
 def test_missing_file(lib, tmp_path):
     with pytest.raises(SegscanError) as e:
         mtx.read(tmp_path / "absent.mtx")
