@@ -14,6 +14,23 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def pytest_sessionstart(session):
+    """Compiles the in-tree CUDA library when it is missing or older than any
+    of its sources (nvcc cross-compiles for sm_103a without a GPU; an
+    up-to-date library costs a few file stats), so the tests always load a
+    library built from the sources they test.  A failed build is reported
+    here and the run goes on: the tests that need the library then fail on
+    loading it, the others still run.  Parallel workers leave it to the
+    controlling process."""
+    if hasattr(session.config, "workerinput"):
+        return
+    from segscan_gb300 import build
+    try:
+        build.build(verbose=True)
+    except Exception as exc:  # reported, never hidden: loading the library fails next
+        print(f"\nsegscan_gb300 library build failed: {exc}", file=sys.stderr)
+
+
 @pytest.fixture(scope="session")
 def oracle():
     import oracle_lib
