@@ -252,15 +252,23 @@ def _errors(C, C64, absC):
             "max_abs_over_max_ref": float(err.max() / max(np.abs(C64).max(), 1e-300))}
 
 
+def _f64_product(A, B):
+    """C = A @ B and |A| @ |B| in FP64 on the host (scipy's CSR product),
+    the exact-enough reference the precision errors are measured against."""
+    import numpy as np
+    import scipy.sparse as sp
+    M = sp.csr_matrix((A.values.astype(np.float64), A.indices, A.indptr), shape=(A.nrow, A.ncol))
+    B64 = B.astype(np.float64)
+    return np.asarray(M @ B64), np.asarray(abs(M) @ np.abs(B64))
+
+
 def extra_precision(A, B, N, fp32_ms, dev):
     """BF16 / FP16 storage of A.vals and B, FP32 accumulation (Kahan on rows
     above 1024 nonzeros), on the power-law matrix: throughput beside plain
     FP32, and error against FP64 on the FP32 inputs."""
     import torch
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle_lib
     from segscan_gb300 import api, autotune, synth
-    C64, absC = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B)
+    C64, absC = _f64_product(A, B)
     out = {}
     stream = torch.cuda.current_stream(dev)
     for name, dt, cdt in (("bf16_c_f32", torch.bfloat16, torch.float32), ("bf16_c_bf16", torch.bfloat16, torch.bfloat16),
@@ -277,7 +285,7 @@ def extra_precision(A, B, N, fp32_ms, dev):
                      "knobs": k.as_dict(), **_errors(Cd.float().cpu().numpy(), C64, absC)}
     # the same at N = 128 (B and C twice as wide), against the FP32 time there
     B128 = synth.dense(A.ncol, 128, seed=2)
-    C64, absC = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B128)
+    C64, absC = _f64_product(A, B128)
     A32 = api.CsrMatrix.from_host(A, dev)
     B32 = torch.from_numpy(B128).to(dev)
     s32, k32 = autotune.best(A32, 128, B32)
