@@ -1,5 +1,5 @@
-"""Rank body for the world-size-2 gloo tests of segscan_gb300.partition
-(spawned processes; CPU only)."""
+"""Rank body for the gloo tests of segscan_gb300.partition (spawned
+processes; CPU only)."""
 import os
 
 import numpy as np
@@ -7,12 +7,22 @@ import torch
 import torch.distributed as dist
 
 
-def run(rank: int, world: int, port: int, out_dir: str) -> None:
+def matrix(case: str):
+    """The sharded matrix: a power-law one, or two rows (with more ranks
+    than rows, some ranks hold an empty shard)."""
+    from segscan_gb300 import synth
+    if case == "two_rows":
+        return synth.Csr(2, 5, np.array([0, 3, 5], np.int32), np.array([0, 2, 4, 1, 4], np.int32),
+                         np.array([0.5, -1.0, 2.0, 1.5, -0.25], np.float32))
+    return synth.powerlaw(3000, 2500, 2.1, 1, 400, seed=17)
+
+
+def run(rank: int, world: int, port: int, out_dir: str, case: str = "powerlaw") -> None:
     import oracle_lib
     from segscan_gb300 import partition, synth
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     try:
-        csr = synth.powerlaw(3000, 2500, 2.1, 1, 400, seed=17)
+        csr = matrix(case)
         N = 8
         B = synth.dense(csr.ncol, N, seed=18)
         dC = synth.dense(csr.nrow, N, seed=19)

@@ -48,11 +48,15 @@ def free_port():
         return s.getsockname()[1]
 
 
-def test_gloo_world2_forward_and_backward(tmp_path):
+@pytest.mark.parametrize("world, case", [(2, "powerlaw"), (3, "two_rows")])
+def test_gloo_forward_and_backward(tmp_path, world, case):
+    """Ranks as gloo processes: the gathered C equals the unsharded one bit
+    for bit and the all-reduced dB equals the unsharded FP64 product, also
+    with more ranks than rows (a rank with an empty shard)."""
     import dist_worker
-    torch.multiprocessing.start_processes(dist_worker.run, args=(2, free_port(), str(tmp_path)), nprocs=2,
-                                          join=True, start_method="spawn")
-    csr = synth.powerlaw(3000, 2500, 2.1, 1, 400, seed=17)
+    torch.multiprocessing.start_processes(dist_worker.run, args=(world, free_port(), str(tmp_path), case),
+                                          nprocs=world, join=True, start_method="spawn")
+    csr = dist_worker.matrix(case)
     B = synth.dense(csr.ncol, 8, seed=18)
     dC = synth.dense(csr.nrow, 8, seed=19)
     full = oracle_lib.spmm_check_f32(csr.indptr, csr.indices, csr.values, B)
