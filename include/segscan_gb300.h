@@ -175,7 +175,8 @@ ss_status ss_spmm_ebsr(const ss_csr *A, int N, const void *B, void *C,
  * 16 MiB array inside the library (held on every GPU that loads it); calls
  * needing more get SS_ERR_CAPACITY.  All calls on a device share that array,
  * so calls that overlap on the GPU race.  The first call on a device looks
- * up the array's address; make it before any stream capture.  No
+ * up the array's address and keeps it; make it before any stream capture,
+ * and do not call this again on a device after cudaDeviceReset.  No
  * counterpart in the reference. */
 ss_status ss_spmm_ebsr_noalloc(const ss_csr *A, int N, const void *B, void *C,
                                int c_dtype, int accumulate,

@@ -23,7 +23,10 @@
 //    call's contents are never used;
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    before any stream capture.  The address is kept for the life of the
+//    process: after cudaDeviceReset the array may live elsewhere, so a
+//    process that resets a device does not call this entry point on it
+//    again.
 #include <mutex>
 
 #include "internal.h"
