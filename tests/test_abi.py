@@ -137,6 +137,42 @@ def test_launch_stream_argument_found_by_position_and_keyword(monkeypatch):
     assert seen == [None, "s1", "s2"]
 
 
+C_CALLER = r"""
+#include <string.h>
+#include "segscan_gb300.h"
+int main(void) {
+  ss_knobs k;
+  if (ss_default_knobs(SS_EBSR, 64, &k) != SS_OK) return 1;
+  if (strcmp(ss_status_string(SS_ERR_CAPACITY), "ok") == 0) return 2;
+  return ss_version() >= 1 ? 0 : 3;
+}
+"""
+
+
+def test_headers_compile_for_plain_c_and_cpp_callers(lib, tmp_path):
+    """include/segscan_gb300.h is plain C: a C99 program that includes it
+    (pedantic, warnings as errors, no CUDA headers) links against the library
+    and runs on a machine without a GPU; the C++ header compiles with the
+    host C++ compiler alone."""
+    import shutil
+    import subprocess
+    from segscan_gb300 import _lib
+    if shutil.which("gcc") is None or shutil.which("g++") is None:
+        pytest.skip("no host C/C++ compiler")
+    inc = str(Path(__file__).resolve().parent.parent / "include")
+    src, exe = tmp_path / "caller.c", tmp_path / "caller"
+    src.write_text(C_CALLER)
+    libdir = str(_lib.LIB_PATH.parent)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", inc, str(src), "-o", str(exe),
+                    "-L", libdir, "-lsegscan_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    assert subprocess.run([str(exe)]).returncode == 0
+    cpp = tmp_path / "caller.cpp"
+    cpp.write_text('#include "segscan_gb300.hpp"\nint main() { return 0; }\n')
+    cuda_inc = Path(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc").resolve().parent.parent / "include"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", inc, "-I", str(cuda_inc),
+                    str(cpp)], check=True)
+
+
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "nope.so")
