@@ -128,6 +128,12 @@ class CsrMatrix:
         return CsrMatrix(self.nrow, self.ncol, self.indptr, self.indices, values)
 
     def descr(self) -> SsCsr:
+        # the C ABI sees only pointers and sizes: tensors shorter than the
+        # sizes claim would be read past their ends on the device
+        if self.indptr.numel() != self.nrow + 1:
+            raise ValueError(f"indptr must hold nrow + 1 = {self.nrow + 1} entries, got {self.indptr.numel()}")
+        if self.values is not None and self.values.numel() != self.nnz:
+            raise ValueError(f"values must hold nnz = {self.nnz} entries (as indices), got {self.values.numel()}")
         _need_cuda("indptr", self.indptr, torch.int32)
         _need_cuda("indices", self.indices, torch.int32)
         if self.values is not None:

@@ -189,6 +189,10 @@ def test_python_api_refuses_host_tensors_and_bad_shapes(lib):
     A = api.CsrMatrix(2, 2, indptr, indices, torch.ones(2))
     with pytest.raises(ValueError, match="CUDA"):
         A.descr()
+    with pytest.raises(ValueError, match="nrow \\+ 1"):
+        api.CsrMatrix(3, 2, indptr, indices, torch.ones(2)).descr()
+    with pytest.raises(ValueError, match="values must hold nnz"):
+        api.CsrMatrix(2, 2, indptr, indices, torch.ones(3)).descr()
     with pytest.raises(ValueError, match="B must be"):
         api.spmm(A, torch.ones(3, 4), "ebsr")
     with pytest.raises(ValueError, match="CUDA"):
