@@ -539,6 +539,8 @@ def coo_to_csr(nrow: int, rows: torch.Tensor, cols: torch.Tensor, ncol: Optional
 
 @_allocates_on_launch_stream
 def gather_values(values: torch.Tensor, perm: torch.Tensor, stream=None) -> torch.Tensor:
+    if perm.numel() != values.numel():  # out has values' length and takes one entry per perm entry
+        raise ValueError(f"perm ({perm.numel()}) and values ({values.numel()}) differ in length")
     _need_cuda("values", values)
     _need_cuda("perm", perm, torch.int32)
     out = _output(values.shape, values.dtype, values.device)
