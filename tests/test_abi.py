@@ -195,6 +195,8 @@ def test_python_api_refuses_host_tensors_and_bad_shapes(lib):
         api.CsrMatrix(2, 2, indptr, indices, torch.ones(3)).descr()
     with pytest.raises(ValueError, match="differ in length"):
         api.gather_values(torch.ones(2), torch.zeros(3, dtype=torch.int32))
+    with pytest.raises(ValueError, match="out must be"):
+        api.segment(torch.ones(2, 4), torch.zeros(2, dtype=torch.int32), 3, out=torch.zeros(2, 4))
     with pytest.raises(ValueError, match="B must be"):
         api.spmm(A, torch.ones(3, 4), "ebsr")
     with pytest.raises(ValueError, match="CUDA"):
