@@ -349,13 +349,13 @@ def segment(src: torch.Tensor, index: torch.Tensor, dst_len: int, reduce: str = 
     + 256 bytes, else one is allocated per call."""
     if src.dim() != 2 or index.dim() != 1 or index.shape[0] != src.shape[0]:
         raise ValueError("src must be [nnz, N] and index [nnz]")
+    nnz, N = int(src.shape[0]), int(src.shape[1])
+    if out is not None and tuple(out.shape) != (int(dst_len), N):
+        raise ValueError(f"out must be [{int(dst_len)}, {N}], got {tuple(out.shape)}")
     _need_cuda("src", src)
     _need_cuda("index", index, torch.int32)
-    nnz, N = int(src.shape[0]), int(src.shape[1])
     if out is None:
         out = _output((dst_len, N), torch.float32, src.device)
-    if tuple(out.shape) != (int(dst_len), N):
-        raise ValueError(f"out must be [{int(dst_len)}, {N}], got {tuple(out.shape)}")
     _need_cuda("out", out, torch.float32)
     ws = workspace if workspace is not None else _workspace(segment_workspace_size(nnz, N, strategy, knobs),
                                                              src.device)
