@@ -117,9 +117,14 @@ const char *ss_status_string(int status);  /* static string */
 /* Text of the last failure on the calling host thread ("" if none). */
 const char *ss_last_error(void);
 /* Device-side status of the bounded waits in the kernels: *status gets 0 or
- * SS_ERR_TIMEOUT (a wait gave up and its chunk was skipped).  clear = 1
- * resets it.  Synchronous with respect to the device.  No counterpart in the
- * reference (its kernels never wait). */
+ * SS_ERR_TIMEOUT (a wait gave up and the group that waited stopped, leaving
+ * its outputs unwritten).  clear = 1 resets it.  Synchronous with respect to
+ * the device.  The flag is one word per device, shared by every launch on
+ * every stream and host thread of the process: a timeout on one stream is
+ * seen by whichever caller reads next, and a clear by one thread can erase a
+ * timeout another thread has not read yet, so callers that share a device
+ * read and clear it at a point where they have ordered their launches.  No
+ * counterpart in the reference (its kernels never wait). */
 ss_status ss_device_error(int *status, int clear);
 /* Diagnostic: one bounded mbarrier wait that can never complete (an
  * expected transaction no copy delivers) gives up after `polls` tries and

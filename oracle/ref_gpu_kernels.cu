@@ -1,8 +1,8 @@
 // The reference's own SpMM kernels (test-cg/include/spmm/spmm_cg.cuh) and
 // the dgSPARSE baseline kernels it includes (spmm.cuh), compiled for sm_103a into a device-only cubin with plain extern "C"
-// entry names, so bench.py can time them on the same GPU as this library
-// through the CUDA driver API.  MEASUREMENT INFRASTRUCTURE ONLY: built by
-// `make refgpu` from the reference sources where they lie (REF=<checkout>),
+// entry names, so the tests (tests/ref_kernels.py) can check and time them
+// on the same GPU as this library through the CUDA driver API.  MEASUREMENT INFRASTRUCTURE ONLY: built by
+// `make ref` from the reference sources where they lie (REF=<checkout>),
 // output in oracle/_ref/ (never committed); nothing here is product code.
 //
 // The reference kernels are __global__ templates.  Its headers are

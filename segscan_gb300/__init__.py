@@ -20,7 +20,7 @@ def load():
 
 def __getattr__(name):
     # torch-dependent modules load lazily so C-ABI checks work without CUDA
-    if name in ("api", "autograd", "autotune", "batched", "partition", "mtx", "workloads"):
+    if name in ("api", "autograd", "autotune", "batched", "partition", "mtx"):
         import importlib
         return importlib.import_module(f".{name}", __name__)
     raise AttributeError(name)

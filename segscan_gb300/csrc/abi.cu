@@ -179,10 +179,10 @@ ss_status geom_sr(long long worker_units, int nnz, int N, int dtype, int val_byt
   g.chunk = k.thread_nz * G;
   // A group pays a chain of dependent loads to set up each chunk (first
   // row search, first staged tile, row window), so chunks much smaller than
-  // the balanced share (nnz over the groups of one full wave on the 152 SMs
-  // at the walk's 1024 resident threads per SM) are merged up to that share:
-  // small thread_nz tuples then run as fast as tuned ones.
-  const long long wave_groups = 152LL * 1024 / G;
+  // the balanced share (nnz over the groups of one full wave on the
+  // device's SMs at the walk's 1024 resident threads per SM) are merged up
+  // to that share: small thread_nz tuples then run as fast as tuned ones.
+  const long long wave_groups = (long long)sm_count() * 1024 / G;
   long long share = nnz > 0 ? ceil_div((long long)nnz, wave_groups) : 0;
   share = ceil_div(share, 32LL) * 32;  // a multiple of 8 keeps the bulk copies 16-byte aligned
   if (share > g.chunk && share <= (1LL << 30)) g.chunk = (int)share;
@@ -231,12 +231,12 @@ static ss_status geom_pr(long long worker_units, int nnz, int N, int dtype, cons
   if (steps < 1) steps = 1;
   g.chunk = (int)(steps * tile);
   // chunks below the share of one full wave (1024 resident threads on each
-  // of the 152 SMs, shared by the column tiles) are merged up to it: each
+  // of the device's SMs, shared by the column tiles) are merged up to it: each
   // chunk costs a chain of dependent loads to set up (cf. geom_sr)
   {
     long long blocks_per_sm = 1024 / g.block;
     if (blocks_per_sm < 1) blocks_per_sm = 1;
-    long long wave = 152LL * blocks_per_sm * g.workers_per_block / (g.cs.tiles > 0 ? g.cs.tiles : 1);
+    long long wave = (long long)sm_count() * blocks_per_sm * g.workers_per_block / (g.cs.tiles > 0 ? g.cs.tiles : 1);
     if (wave < 1) wave = 1;
     long long share = nnz > 0 ? ceil_div((long long)nnz, wave) : 0;
     share = ceil_div(share, (long long)tile) * tile;
@@ -270,9 +270,12 @@ static ss_status check_csr(const ss_csr *A, int N) {
   return SS_OK;
 }
 
+// The caller's knobs, or the strategy's defaults; null (with the failure
+// recorded) for an unknown strategy.
 static const ss_knobs *knobs_or_default(int strategy, int N, const ss_knobs *k, ss_knobs &tmp) {
   if (k) return k;
-  ss_default_knobs(strategy, N, &tmp);
+  memset(&tmp, 0, sizeof(tmp));
+  if (ss_default_knobs(strategy, N, &tmp) != SS_OK) return nullptr;
   return &tmp;
 }
 
@@ -391,6 +394,7 @@ ss_status ss_spmm_workspace_size(int strategy, const ss_csr *A, int N, const ss_
   if (st) return st;
   ss_knobs tmp;
   const ss_knobs *k = knobs_or_default(strategy, N, knobs, tmp);
+  if (!k) return SS_ERR_INVALID_ARG;
   SpmmCall c;
   c.M = A->nrow; c.K = A->ncol; c.N = N; c.nnz = A->nnz; c.val_dtype = A->value_dtype;
   RbGeom rg;
@@ -406,6 +410,7 @@ ss_status ss_spmm(int strategy, const ss_csr *A, int N, const void *B, void *C, 
   ss::NvtxRange nvtx_range("ss_spmm");
   ss_knobs tmp;
   const ss_knobs *k = knobs_or_default(strategy, N, knobs, tmp);
+  if (!k) return SS_ERR_INVALID_ARG;
   SpmmCall c;
   ss_status st = make_spmm_call(strategy, A, N, B, C, c_dtype, accumulate, *k, c);
   if (st) return st;

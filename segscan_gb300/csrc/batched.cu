@@ -9,13 +9,6 @@ namespace ss {
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static int sm_count_batched() {
-  int dev = 0, n = 0;
-  cudaGetDevice(&dev);
-  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
-  return n;
-}
-
 // Fills h (everything but the offsets' final sizes) and per-matrix chunk
 // sizes; returns the number of items.
 static ss_status batch_layout(int count, const ss_csr *mats, int N, const ss_knobs *per_mat, BatchHeader &h,
@@ -165,7 +158,7 @@ ss_status ss_spmm_batched(const void *host_plan, void *dev_plan, void *stream) {
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, h.block, h.smem);
   if (e != cudaSuccess || per_sm < 1) return fail(SS_ERR_UNSUPPORTED_KNOBS, "batched block does not fit an SM");
-  long long grid = (long long)per_sm * sm_count_batched();
+  long long grid = (long long)per_sm * sm_count();
   const long long need = ((long long)h.total_items + h.workers_per_block - 1) / h.workers_per_block;
   if (grid > need) grid = need;
   // arrival counts and work counters (adjacent in the plan)

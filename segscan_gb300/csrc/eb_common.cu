@@ -80,7 +80,7 @@ ss_status launch_fixup(const CarryView &cv, int num_chunks, int N, int M, void *
                        int reduce, int accumulate, const int32_t *index, int nnz, cudaStream_t s) {
   if (num_chunks <= 1 || N == 0 || M == 0) return SS_OK;  // chunk 0 never carries
   const int threads = 256;
-  const int blocks = std::max(1, std::min((num_chunks + 7) / 8, 152 * 32));
+  const int blocks = std::max(1, std::min((num_chunks + 7) / 8, sm_count() * 32));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks, 1, 1);
   cfg.blockDim = dim3(threads, 1, 1);

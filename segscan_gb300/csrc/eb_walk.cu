@@ -1,4 +1,6 @@
 // Launchers of the sequential-walk kernels (templates in eb_walk.cuh).
+#include <mutex>
+
 #include "eb_walk.cuh"
 
 namespace ss {
@@ -7,10 +9,15 @@ namespace ss {
 __device__ int g_walk_error;
 
 int *walk_error_ptr() {
+  static std::mutex mu;
   static int *p[64] = {nullptr};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  if (!p[dev] && cudaGetSymbolAddress((void **)&p[dev], g_walk_error) != cudaSuccess) p[dev] = nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!p[dev]) {
+    int *q = nullptr;
+    if (cudaGetSymbolAddress((void **)&q, g_walk_error) == cudaSuccess) p[dev] = q;
+  }
   return p[dev];
 }
 
@@ -21,16 +28,6 @@ EbArgs eb_base_args(const EbGeom &g, void *ws, int N);
 
 size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes) {
   return (size_t)workers_per_block * (size_t)sr_layout(stage, val_bytes).bytes;
-}
-
-static int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
-  }
-  return n;
 }
 
 static ss_status run_sr(void *fn, EbArgs &a, const EbGeom &g, size_t smem, cudaStream_t s, const char *what) {

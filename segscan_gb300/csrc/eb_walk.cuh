@@ -22,9 +22,10 @@
 //    store, head/tail slots for the two rows that straddle the chunk,
 //    zeros for empty rows).
 // Every wait on an mbarrier is bounded; on expiry the kernel records
-// SS_ERR_TIMEOUT in the device flag a.err (ss_device_error) and skips the
-// chunk.  This header holds the kernel templates; eb_walk_*.cu instantiate
-// them per storage type and eb_walk.cu launches them.
+// SS_ERR_TIMEOUT in the device flag a.err (ss_device_error) and the group
+// stops walking: it waits (bounded) for the copies it has in flight and
+// issues no more.  This header holds the kernel templates; eb_walk_*.cu
+// instantiate them per storage type and eb_walk.cu launches them.
 #pragma once
 #include "eb_common.cuh"
 #include "internal.h"
@@ -103,22 +104,32 @@ __device__ __forceinline__ void stage_issue(const EbArgs &a, Stage &st, const Sr
   }
 }
 
-// Waits for buffer b; false when the bounded wait expired.
+// Waits for buffer b; false when the bounded wait expired.  The group
+// agrees on the outcome; the phase advances only on success, so a buffer
+// whose wait expired can be waited for again (stage_drain).
 __device__ __forceinline__ bool stage_wait(Stage &st, int b, unsigned mask, int *err) {
   bool ok = true;
   if (st.tma & (1u << b)) {
     uint32_t it = 0;
     while (!mbar_try_wait(st.bar + b, (st.phases >> b) & 1u)) {
       if (++it > SR_SPIN_LIMIT) {
-        if (err) atomicExch(err, (int)SS_ERR_TIMEOUT);
         ok = false;
         break;
       }
     }
-    st.phases ^= 1u << b;
+    ok = __all_sync(mask, ok);
+    if (ok) st.phases ^= 1u << b;
+    else if (err) atomicExch(err, (int)SS_ERR_TIMEOUT);
   }
   __syncwarp(mask);
   return ok;
+}
+
+// After an expired wait: waits again, bounded, for the staged tiles
+// [from, to) whose bulk copies may still be landing, so the group leaves no
+// copy in flight into its buffers.
+__device__ __forceinline__ void stage_drain(Stage &st, int from, int to, unsigned mask) {
+  for (int t = from; t < to; t++) stage_wait(st, t & 1, mask, nullptr);
 }
 
 template <int V, int NV, bool KAHAN>
@@ -241,7 +252,10 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
     const int sb = ci.cs + s * L.S;
     const int n = min(L.S, ci.ce - sb);
     const int last = sb + n - 1;
-    if (!stage_wait(st, b, mask, a.err)) return false;
+    if (!stage_wait(st, b, mask, a.err)) {
+      stage_drain(st, s, min(nst, s + 2), mask);  // tiles s and s + 1 may still be landing
+      return false;
+    }
     const int32_t *scol = st.col + b * L.S;
     const T *sval = reinterpret_cast<const T *>(st.val + b * L.S * L.vs);
     int32_t *sinfo = st.info + b * L.S;
@@ -430,8 +444,9 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
 // segment_coo chunk walk: segment ids come from the staged sorted index,
 // src rows are streamed in order
 // ---------------------------------------------------------------------
+// Returns false when a bounded wait expired (the caller then stops).
 template <typename T, int V, int NV, bool KAHAN>
-__device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
+__device__ __forceinline__ bool sr_seg_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
                                              const SrLayout &L, int col0, const bool (&act)[NV], uint64_t strm) {
   const T *__restrict__ src = (const T *)a.B;
   const int G = a.team_lanes;
@@ -467,7 +482,10 @@ __device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lan
     const int b = s & 1;
     const int sb = ci.cs + s * L.S;
     const int n = min(L.S, ci.ce - sb);
-    if (!stage_wait(st, b, mask, a.err)) return;
+    if (!stage_wait(st, b, mask, a.err)) {
+      stage_drain(st, s, min(nst, s + 2), mask);  // tiles s and s + 1 may still be landing
+      return false;
+    }
     const int32_t *sidx = st.col + b * L.S;
     for (int q = 0; q < n; q += SR_U) {
       float bv[SR_U][NV][V];
@@ -534,6 +552,7 @@ __device__ __forceinline__ void sr_seg_chunk(const EbArgs &a, int chunk, int lan
     if (mean && lane == 0) a.seg_cnt[chunk] = cnt;
     seg_carry_arrive<V, NV>(a, cur, chunk, l, lane, G, mask, col0, act, strm);
   }
+  return true;
 }
 
 template <typename T, typename TC, int V, int NV, bool SEG>
@@ -569,14 +588,17 @@ __global__ void __launch_bounds__(512, SS_SR_MIN_BLOCKS) eb_sr_kernel(EbArgs a) 
   const bool kahan = a.chunk > a.kahan;
   const int stride = gridDim.x * a.workers_per_block;
   for (int chunk = blockIdx.x * a.workers_per_block + wib; chunk < a.num_chunks; chunk += stride) {
+    bool ok;
     if (SEG) {
-      if (kahan) sr_seg_chunk<T, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, strm);
-      else sr_seg_chunk<T, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, strm);
+      ok = kahan ? sr_seg_chunk<T, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, strm)
+                 : sr_seg_chunk<T, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, strm);
     } else {
-      const bool ok = kahan ? sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm)
-                            : sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
-      if (!ok) break;  // a bounded wait expired: copies may still be landing in this group's buffers
+      ok = kahan ? sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm)
+                 : sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
     }
+    // a bounded wait expired: the group waited again for its copies in
+    // flight and issues nothing more into its buffers
+    if (!ok) break;
   }
   // every issued stage was waited for: no bulk copy is in flight here
 }

@@ -97,6 +97,9 @@ size_t sr_smem_bytes(int stage, int workers_per_block, int val_bytes);
 void *narrow_kernel(int val_dtype, int c_dtype, int V, int NV);
 // device address of the bounded-wait status word (eb_walk.cu)
 int *walk_error_ptr();
+// streaming multiprocessors of the current device, looked up once per device
+// (util.cu); 1 when the query fails
+int sm_count();
 
 // Launchers (kernels live in spmm_rb.cu, eb_walk.cu, eb_scan.cu).
 ss_status launch_rbsr(const SpmmCall &c, const RbGeom &g, cudaStream_t s);

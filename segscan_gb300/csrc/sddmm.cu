@@ -131,7 +131,7 @@ extern "C" ss_status ss_sddmm(const ss_csr *A, int N, const float *dC, const voi
   const int threads = 256;
   const long long teams_needed = ((long long)nnz + SDDMM_CHUNK - 1) / SDDMM_CHUNK;
   long long blocks = (teams_needed * lanes + threads - 1) / threads;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks > (long long)sm_count() * 16) blocks = (long long)sm_count() * 16;
   if (blocks < 1) blocks = 1;
   int log2_lanes = ilog2(lanes);
   int M = A->nrow, K = A->ncol, Nn = N, nz = nnz;

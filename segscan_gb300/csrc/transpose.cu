@@ -63,7 +63,7 @@ static size_t transpose_ws_bytes(int K, int nnz, TransposeWs *w, void *base) {
 
 static int grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
-  if (b > 152 * 32) b = 152 * 32;
+  if (b > (long long)sm_count() * 32) b = (long long)sm_count() * 32;
   return b < 1 ? 1 : (int)b;
 }
 
@@ -300,7 +300,7 @@ static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out
   sort_small_kernel<<<grid_for(K, 256), 256, 0, s>>>(out_indptr, K, perm, w.work);
   e = cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_SORT_MAX * 4);
   if (e != cudaSuccess) return cuda_fail(e, "counting sort attribute");
-  sort_large_kernel<<<2 * 152, 1024, SMEM_SORT_MAX * 4, s>>>(out_indptr, perm, w.work);
+  sort_large_kernel<<<2 * sm_count(), 1024, SMEM_SORT_MAX * 4, s>>>(out_indptr, perm, w.work);
   e = cudaGetLastError();
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "counting sort launch");
 }

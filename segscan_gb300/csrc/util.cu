@@ -1,8 +1,25 @@
 // Row assignment, input validation and value gather.
+#include <atomic>
+
 #include "common.cuh"
 #include "internal.h"
 
 namespace ss {
+
+int sm_count() {
+  static std::atomic<int> cache[64];  // 0 = not looked up yet
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (dev < 0 || dev >= 64) {
+    int n = 0;
+    return cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 1;
+  }
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 1;
+  cache[dev].store(n, std::memory_order_relaxed);  // every thread stores the same value
+  return n;
+}
 
 // rows[i] = binary_search_segment_number(indptr, M, nnz, e) for e = elems[i]
 // (test-cg/include/util/check.cuh:88-102), or for e = i when elems is null.
@@ -52,7 +69,8 @@ __global__ void gather_kernel(const T *__restrict__ in, const int32_t *__restric
 
 static int grid_for(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
-  if (b > 152 * 32) b = 152 * 32;
+  const int64_t cap = (int64_t)sm_count() * 32;
+  if (b > cap) b = cap;
   return b < 1 ? 1 : (int)b;
 }
 

@@ -1,7 +1,9 @@
-"""Named single-kernel workloads: run one case a few times and print its
-device time and algorithmic throughput (GB/s of the bytes the operation must
-move).  Used to measure and profile each kernel of the library on the
-synthetic matrices the benchmark configurations name.
+"""Profiling reproducer (measurement infrastructure, not part of the
+library's API and not imported by the package): named single-kernel
+workloads that run one case a few times and print its device time and
+algorithmic throughput (GB/s of the bytes the operation must move).  The
+commands of the ncu summaries under profiles/ run it, so each summary can be
+reproduced on the synthetic matrices the benchmark configurations name.
 
     python -m segscan_gb300.workloads <case> [--iters K] [--scale S]
 

@@ -16,6 +16,7 @@ holds the inputs and the reference's outputs.
 from __future__ import annotations
 
 import argparse
+import os
 import ctypes
 import subprocess
 import sys
@@ -89,7 +90,8 @@ def edge_matrix(seed: int = 7) -> synth.Csr:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("SEGSCAN_REF"),
+                    help="the reference checkout (default: $SEGSCAN_REF)")
     args = ap.parse_args()
     lib = load_ref(args.ref)
 

@@ -235,7 +235,8 @@ def test_small_chunks_merge_to_the_wave_share(cuda):
     B = torch.from_numpy(synth.dense(csr.ncol, 64, seed=32)).cuda()
     A = dev_csr(csr)
     G = 16
-    share = -(-csr.nnz // (152 * 1024 // G))
+    sms = torch.cuda.get_device_properties(0).multi_processor_count  # the device's wave, as the library reads it
+    share = -(-csr.nnz // (sms * 1024 // G))
     share = -(-share // 32) * 32
     assert share % G == 0
     tiny = spmm(A, B, "ebsr", knobs=api.make_knobs("ebsr", 64, group_factor=4, thread_nz=1, block_denom=1))

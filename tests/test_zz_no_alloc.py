@@ -47,9 +47,10 @@ def test_noalloc_rejects_oversize_scratch(lib):
     """A call whose scratch would exceed the fixed array is refused before any
     device work (the pointers here are never dereferenced)."""
     big = SsCsr(4_000_000, 4_000_000, 400_000_000, 256, 512, 1024, 0)
-    knobs = SsKnobs(4, 0, 256, 1, 1, 4, 1, 0)
-    # ~9.7 K chunks (one wave's share each) of 1024-wide head and tail
-    # partials: ~80 MB of carries
-    st = lib.ss_spmm_ebsr_noalloc(ctypes.byref(big), 1024, 4096, 8192, 0, 0, ctypes.byref(knobs), None)
+    knobs = SsKnobs(0, 0, 256, 1, 1, 4, 1, 0)
+    # one-lane groups: at least 1024 chunks (one wave's share each, 1024
+    # groups per SM on any SM count) of 4096-wide head and tail partials,
+    # 32 KB per chunk: 32 MB of carries or more
+    st = lib.ss_spmm_ebsr_noalloc(ctypes.byref(big), 4096, 4096, 8192, 0, 0, ctypes.byref(knobs), None)
     assert st == Status.CAPACITY
     assert b"fixed" in lib.ss_last_error()
