@@ -168,6 +168,67 @@ EXPORT void oracle_spmm_f64(int M, int N, const int32_t *indptr,
   }
 }
 
+/* Row-parallel form of oracle_spmm_f64 for the full-size parity checks.
+ * Rows are independent and keep the sequential order, so the result is
+ * bit-identical for any thread count. */
+typedef struct {
+  int64_t r0, r1;
+  int N;
+  const int32_t *indptr, *indices;
+  const float *vals, *B;
+  double *C, *Cabs;
+} spmm64_job;
+
+static void *spmm64_job_run(void *arg) {
+  spmm64_job *j = (spmm64_job *)arg;
+  const int64_t N = j->N;
+  /* indptr holds absolute positions into indices, so the row block only
+   * shifts indptr and the outputs */
+  oracle_spmm_f64((int)(j->r1 - j->r0), j->N, j->indptr + j->r0, j->indices, j->vals, j->B,
+                  j->C + j->r0 * N, j->Cabs ? j->Cabs + j->r0 * N : NULL);
+  return NULL;
+}
+
+EXPORT void oracle_spmm_f64_mt(int M, int N, const int32_t *indptr, const int32_t *indices,
+                               const float *vals, const float *B, double *C, double *Cabs,
+                               int nthreads) {
+  if (nthreads <= 1 || M < 2 * nthreads) {
+    oracle_spmm_f64(M, N, indptr, indices, vals, B, C, Cabs);
+    return;
+  }
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  int started[256];
+  spmm64_job jobs[256];
+  int64_t nnz = indptr[M];
+  int64_t r = 0;
+  for (int t = 0; t < nthreads; t++) {
+    int64_t target = (nnz * (t + 1)) / nthreads;
+    int64_t r1;
+    if (t == nthreads - 1) {
+      r1 = M;
+    } else {
+      int64_t lo = r, hi = M;
+      while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (indptr[mid + 1] <= target) lo = mid + 1; else hi = mid;
+      }
+      r1 = lo + 1 > M ? M : lo + 1;
+      if (r1 < r) r1 = r;
+    }
+    jobs[t].r0 = r; jobs[t].r1 = r1; jobs[t].N = N;
+    jobs[t].indptr = indptr; jobs[t].indices = indices; jobs[t].vals = vals; jobs[t].B = B;
+    jobs[t].C = C; jobs[t].Cabs = Cabs;
+    r = r1;
+  }
+  for (int t = 0; t < nthreads; t++) {
+    started[t] = pthread_create(&th[t], NULL, spmm64_job_run, &jobs[t]) == 0;
+    if (!started[t]) spmm64_job_run(&jobs[t]);
+  }
+  for (int t = 0; t < nthreads; t++)
+    if (started[t]) pthread_join(th[t], NULL);
+}
+
 /* ------------------------------------------------------------------ */
 /* Row of a nonzero: upper_bound(indptr[1..M-1], e) - 1.               */
 /* Empty rows are skipped; e >= nnz gives M-1 (check.cuh:88-102).      */

@@ -62,16 +62,21 @@ def spmm_check_f32(indptr, indices, vals, B, threads: int = 1, out=None):
     return out
 
 
-def spmm_f64(indptr, indices, vals, B):
-    """(C64, |A||B|) in FP64; vals None means ones."""
+def spmm_f64(indptr, indices, vals, B, threads: int = 1):
+    """(C64, |A||B|) in FP64; vals None means ones.  threads > 1 splits the
+    rows over host threads (the same bits: rows are independent)."""
     M = indptr.size - 1
     N = B.shape[1]
     C = np.empty((M, N), dtype=np.float64)
     A = np.empty((M, N), dtype=np.float64)
-    load().oracle_spmm_f64(c_int(M), c_int(N), _p(np.ascontiguousarray(indptr, np.int32)),
-                           _p(np.ascontiguousarray(indices, np.int32)),
-                           None if vals is None else _p(np.ascontiguousarray(vals, np.float32)),
-                           _p(np.ascontiguousarray(B, np.float32)), _p(C), _p(A))
+    args = (c_int(M), c_int(N), _p(np.ascontiguousarray(indptr, np.int32)),
+            _p(np.ascontiguousarray(indices, np.int32)),
+            None if vals is None else _p(np.ascontiguousarray(vals, np.float32)),
+            _p(np.ascontiguousarray(B, np.float32)), _p(C), _p(A))
+    if threads > 1:
+        load().oracle_spmm_f64_mt(*args, c_int(threads))
+    else:
+        load().oracle_spmm_f64(*args)
     return C, A
 
 

@@ -87,3 +87,14 @@ def test_sddmm_f64():
     rows = np.repeat(np.arange(M), np.diff(g["indptr"]))
     ref = np.einsum("ij,ij->i", dC[rows].astype(np.float64), g["B"][g["indices"]].astype(np.float64))
     assert np.allclose(out, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_spmm_f64_threads_same_bits():
+    """The row-parallel FP64 product used by the full-size parity tests gives
+    the single-thread bits."""
+    from segscan_gb300 import synth
+    A = synth.powerlaw(50000, 40000, 2.1, 1, 3000, seed=12)
+    B = synth.dense(A.ncol, 9, seed=13)
+    c1, a1 = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B)
+    c8, a8 = oracle_lib.spmm_f64(A.indptr, A.indices, A.values, B, threads=8)
+    assert np.array_equal(c1, c8) and np.array_equal(a1, a8)
