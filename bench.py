@@ -262,6 +262,18 @@ def _f64_product(A, B):
     return np.asarray(M @ B64), np.asarray(abs(M) @ np.abs(B64))
 
 
+def _check_output(A, B, C):
+    """The timed C against FP64 (scipy): max |C - C64| / (|A||B|) per element
+    and the normwise error, with the FP32 bar of the parity tests (1e-5)."""
+    import numpy as np
+    C64, absC = _f64_product(A, B)
+    e = _errors(C.cpu().numpy(), C64, absC)
+    return {"max_err": e["max_rel_to_sum_abs"], "normwise_err": e["normwise_rel"], "bar": 1e-5,
+            "pass": bool(e["max_rel_to_sum_abs"] <= 1e-5 and e["normwise_rel"] <= 1e-5
+                         and np.isfinite(e["normwise_rel"])),
+            "against": "FP64 product on the host (scipy), per element relative to sum|a*b|"}
+
+
 def extra_precision(A, B, N, fp32_ms, dev):
     """BF16 / FP16 storage of A.vals and B, FP32 accumulation (Kahan on rows
     above 1024 nonzeros), on the power-law matrix: throughput beside plain
@@ -308,11 +320,13 @@ def extra_precision(A, B, N, fp32_ms, dev):
     return out
 
 
-def extra_batched(dev, N=64, count=512):
+def extra_batched(dev, N=64, count=512, headline=None):
     """512 CSR matrices (rows log-uniform in [100, 50000], row length Zipf 2.3
     clipped to [1, 2000], seed 3): one persistent launch replayed from a CUDA
     graph (BF16 storage, FP32 accumulation) against one plain FP32 launch per
-    matrix."""
+    matrix, and like for like: batched BF16 against batched FP32 on the same
+    matrices, and batched BF16 against the plain FP32 headline SpMM per
+    nonzero (headline = (nnz, ms) of the timed FP32 step)."""
     import numpy as np
     import torch
     from segscan_gb300 import api, autotune, batched, synth
@@ -366,7 +380,15 @@ def extra_batched(dev, N=64, count=512):
             err.append(float((plan.out[i].double() - ref).norm() / max(float(ref.norm()), 1e-300)))
         res[name] = {"ms": ms, "speedup_vs_plain_fp32": plain_ms / ms,
                      "speedup_vs_plain_fp32_graph": plain_graph_ms / ms, "chunk_target": target,
-                     "max_normwise_rel_vs_fp32": max(err)}
+                     "max_normwise_rel_vs_fp32": max(err), "gnnz_per_s": res["nnz"] / ms / 1e6}
+    # like for like: the same batch in FP32 and BF16, and BF16 per nonzero
+    # against the plain FP32 headline SpMM
+    res["bf16_over_fp32_batched"] = res["batched_fp32_graph"]["ms"] / res["batched_bf16_c_f32_graph"]["ms"]
+    if headline is not None:
+        h_nnz, h_ms = headline
+        res["plain_fp32_headline_gnnz_per_s"] = h_nnz / h_ms / 1e6
+        res["batched_bf16_over_plain_fp32_per_nnz"] = (res["batched_bf16_c_f32_graph"]["gnnz_per_s"]
+                                                       / res["plain_fp32_headline_gnnz_per_s"])
     return res
 
 
@@ -377,9 +399,43 @@ def _cusparse_ms(A, B, stream):
     return _event_ms(lambda: torch.sparse.mm(At, B), 10, stream)
 
 
+CUSPARSE_LINE = ROOT / "_build" / "bench_cusparse.so"
+
+
+def _cusparse_direct_ms(A, B, stream, C_ours=None):
+    """cusparseSpMM (CSR, CUSPARSE_SPMM_ALG_DEFAULT) with its handle,
+    descriptors and workspace made once (bench_cusparse.cu, the reference's
+    cuSPARSE call): ms per call, and its normwise difference from C_ours."""
+    import ctypes
+    import torch
+    lib = ctypes.CDLL(str(CUSPARSE_LINE))
+    vp = ctypes.c_void_p
+    lib.csp_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                               ctypes.c_int, vp, vp]
+    lib.csp_run.argtypes = [vp, vp]
+    lib.csp_destroy.argtypes = [vp]
+    N = int(B.shape[1])
+    C = torch.empty((A.nrow, N), device=B.device)
+    h = vp()
+    st = lib.csp_create(ctypes.byref(h), A.nrow, A.ncol, A.nnz, A.indptr.data_ptr(), A.indices.data_ptr(),
+                        A.values.data_ptr(), N, B.data_ptr(), C.data_ptr())
+    if st:
+        raise RuntimeError(f"cuSPARSE setup failed with status {st}")
+    try:
+        s = vp(stream.cuda_stream)
+        ms = _event_ms(lambda: lib.csp_run(h, s), 10, stream)
+        diff = None
+        if C_ours is not None:
+            diff = float((C.double() - C_ours.double()).norm() / max(float(C_ours.double().norm()), 1e-300))
+        return ms, diff
+    finally:
+        lib.csp_destroy(h)
+
+
 def extra_sweep(A_pl, dev):
     """Every configuration's shape through the tuned strategy, with cuSPARSE
-    beside it: power-law 1e6 at N = 4, 16, 64, 128; banded 120k x 120k
+    beside it (cusparseSpMM with handle and descriptors made once, and
+    torch.sparse.mm): power-law 1e6 at N = 4, 16, 64, 128; banded 120k x 120k
     (20 per row, half-width 500) at N = 64; Poisson(16) 4096 x 4096 at
     N = 4, 16 (L2-resident and launch bound: no roofline meaning)."""
     import torch
@@ -404,7 +460,12 @@ def extra_sweep(A_pl, dev):
                  "api": "SpmmPlan.run"}
         try:
             cs = _cusparse_ms(Ad, B, stream)
-            entry.update({"cusparse_ms": cs, "speedup_vs_cusparse": cs / ms})
+            entry.update({"cusparse_torch_ms": cs, "speedup_vs_cusparse_torch": cs / ms})
+        except Exception as exc:
+            entry["cusparse_torch_error"] = f"{type(exc).__name__}: {exc}"
+        try:
+            cd, diff = _cusparse_direct_ms(Ad, B, stream, C_ours=C)
+            entry.update({"cusparse_ms": cd, "speedup_vs_cusparse": cd / ms, "cusparse_normwise_diff": diff})
         except Exception as exc:
             entry["cusparse_error"] = f"{type(exc).__name__}: {exc}"
         res[f"{name}_n{N}"] = entry
@@ -479,22 +540,27 @@ def run_ours(args):
     if ws_ > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
+    from segscan_gb300 import partition
     A, B = workload(args.N)
     N = args.N
-    nbytes = synth.spmm_bytes(A, N)
-    Ad = api.CsrMatrix.from_host(A, dev)
+    nbytes = synth.spmm_bytes(A, N)  # the whole job's algorithmic bytes, over every rank's rows
+    # each rank holds its nnz-balanced row block of A (all of A on one GPU)
+    # and a replicated B, and computes its rows of C with no collective: the
+    # one matrix split over the ranks (strong scaling)
+    S = partition.ShardedSpMM(A, rank, ws_, partition.DeviceKernels(dev))
+    Ah, Ad = S.part, S.A
     Bd = torch.from_numpy(B).to(dev)
     strategy, knobs = choose(args, Ad, N)
-    C = torch.empty((A.nrow, N), dtype=torch.float32, device=dev)
-    wsz = api.spmm_workspace_size(Ad, N, strategy, knobs)
-    work = torch.empty(wsz + 256, dtype=torch.uint8, device=dev) if wsz else None
+    S.kernels.strategy, S.kernels.knobs = strategy, knobs
+    C = torch.empty((Ah.nrow, N), dtype=torch.float32, device=dev)
+    work = S.kernels.workspace(Ad, N)
     stream = torch.cuda.current_stream(dev)
     # ebsr: one walk launch (straddling rows assembled inside it, after a
     # memset of the arrival counts); ebpr: scan + fix-up; row-balanced: one
     kernels_per_step = 2 if strategy == "ebpr" else 1
 
     def step():
-        api.spmm(Ad, Bd, strategy, knobs=knobs, out=C, workspace=work, stream=stream)
+        S.forward(Bd, out=C, workspace=work, stream=stream)
 
     sampler = ClockSampler(local)
     sampler.start()
@@ -523,6 +589,9 @@ def run_ours(args):
         tt = torch.tensor([t], device=dev, dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t = float(tt.item())
+    # the C the timed steps wrote, checked once (outside the timed region)
+    # against an FP64 product on the host, at the FP32 parity bar
+    check = _check_output(Ah, B, C)
 
     # end to end through the public API: host inputs in pinned memory,
     # H2D of A and B, the SpMM, D2H of C, every step.  Copies in, the SpMM
@@ -530,9 +599,9 @@ def run_ours(args):
     # between two device buffer sets, ordered by events: step i's inputs go
     # up while step i-1 computes and step i-2's C comes down, so both link
     # directions stay busy (each step still moves all of its own bytes)
-    h_indptr = torch.from_numpy(A.indptr).pin_memory()
-    h_indices = torch.from_numpy(A.indices).pin_memory()
-    h_values = torch.from_numpy(A.values).pin_memory()
+    h_indptr = torch.from_numpy(Ah.indptr).pin_memory()
+    h_indices = torch.from_numpy(Ah.indices).pin_memory()
+    h_values = torch.from_numpy(Ah.values).pin_memory()
     h_B = torch.from_numpy(B).pin_memory()
     e2e_streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)]  # in, compute, out
     ev_in = [torch.cuda.Event() for _ in range(2)]     # set k's inputs are on the device
@@ -542,9 +611,9 @@ def run_ours(args):
     for _ in range(2):
         d = dict(indptr=torch.empty_like(Ad.indptr), indices=torch.empty_like(Ad.indices),
                  values=torch.empty_like(Ad.values), B=torch.empty_like(Bd), C=torch.empty_like(C),
-                 hC=torch.empty((A.nrow, N), dtype=torch.float32).pin_memory(),
+                 hC=torch.empty((Ah.nrow, N), dtype=torch.float32).pin_memory(),
                  ws=torch.empty_like(work) if work is not None else None)
-        d["A"] = api.CsrMatrix(A.nrow, A.ncol, d["indptr"], d["indices"], d["values"])
+        d["A"] = api.CsrMatrix(Ah.nrow, Ah.ncol, d["indptr"], d["indices"], d["values"])
         sets.append(d)
     h2d = sum(x.numel() * x.element_size() for x in (h_indptr, h_indices, h_values, h_B))
     d2h = sets[0]["hC"].numel() * sets[0]["hC"].element_size()
@@ -630,23 +699,25 @@ def run_ours(args):
     if rank != 0:
         return
     peak, peak_kind = peaks()
-    achieved = nbytes / t / 1e9
+    achieved = nbytes / t / 1e9  # the whole job: every rank's rows in the slowest rank's time
+    per_gpu = achieved / ws_
     kernel_file = f"spmm_{strategy}_powerlaw_n{N}.md"
     line = {
-        "metric": METRIC, "value": achieved * ws_, "unit": UNIT, "n_gpus": ws_, "steps": args.steps,
-        "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": achieved, "unit": UNIT, "n_gpus": ws_, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config(A, N, {"strategy": strategy, "knobs": knobs.as_dict(), "parallelism": f"replica x{ws_}"}),
+        "config": config(A, N, {"strategy": strategy, "knobs": knobs.as_dict(), "parallelism": f"row blocks x{ws_}, B replicated"}),
         "gflops": 2.0 * A.nnz * N / t / 1e9,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind,
+        "roofline": {"bound": "hbm", "achieved": per_gpu, "peak": peak, "unit": "GB/s",
+                     "frac": per_gpu / peak, "peak_kind": peak_kind,
                      "traffic": traffic_from_profiles(kernel_file),
                      "gather_upper_bound_bytes": A.nnz * N * 4 + A.nnz * 8 + (A.nrow + 1) * 4 + A.nrow * N * 4,
                      "kernel": (f"{strategy} SpMM step (walk with in-kernel carry assembly)" if strategy == "ebsr"
                                 else f"{strategy} SpMM step"),
                      "bytes_per_launch": nbytes},
-        "e2e": {"value": nbytes / t_e2e / 1e9 * ws_, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": nbytes / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3, "pinned_copy_gbs": copy_gbs},
+        "check": check,
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clocks,
     }
@@ -654,7 +725,7 @@ def run_ours(args):
         configs = {}
         for key, fn in (("sweep_vs_cusparse", lambda: extra_sweep(A, dev)),
                         ("precision_powerlaw_n64", lambda: extra_precision(A, B, N, t * 1e3, dev)),
-                        ("batched_512", lambda: extra_batched(dev)),
+                        ("batched_512", lambda: extra_batched(dev, headline=(A.nnz, t * 1e3))),
                         ("fwd_bwd_powerlaw_2e6_n128", lambda: extra_fwd_bwd(dev))):
             try:
                 configs[key] = fn()

@@ -40,3 +40,44 @@ def run(rank: int, world: int, port: int, out_dir: str, case: str = "powerlaw") 
             np.save(os.path.join(out_dir, "dB.npy"), dB.numpy())
     finally:
         dist.destroy_process_group()
+
+
+class HostKernels:
+    """ShardedSpMM's per-rank compute on the host with the oracle (the CPU
+    tests have no CUDA kernels): the reference's check-path SpMM forward,
+    FP64 SDDMM and A^T dC backward."""
+
+    def upload(self, csr):
+        return csr
+
+    def spmm(self, A, B, **kw):
+        import oracle_lib
+        return torch.from_numpy(oracle_lib.spmm_check_f32(A.indptr, A.indices, A.values, B))
+
+    def backward(self, A, B, dC):
+        import oracle_lib
+        t_indptr, t_indices, perm = oracle_lib.csr_transpose(A.indptr, A.indices, A.ncol)
+        dB, _ = oracle_lib.spmm_f64(t_indptr, t_indices, A.values[perm], dC)
+        dvals, _ = oracle_lib.sddmm_f64(A.indptr, A.indices, dC, B)
+        return torch.from_numpy(dvals), torch.from_numpy(dB)
+
+
+def run_sharded(rank: int, world: int, port: int, out_dir: str, case: str, compact: bool) -> None:
+    """The same forward and backward through partition.ShardedSpMM."""
+    from segscan_gb300 import partition, synth
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        csr = matrix(case)
+        N = 8
+        B = synth.dense(csr.ncol, N, seed=18)
+        dC = synth.dense(csr.nrow, N, seed=19)
+        S = partition.ShardedSpMM(csr, rank, world, HostKernels(), compact_B=compact)
+        B_local = S.local_B(B)
+        C = S.gather(S.forward(B_local))
+        dvals, dB = S.backward(np.ascontiguousarray(dC[S.r0:S.r1]), B_local)
+        np.save(os.path.join(out_dir, f"dvals_{rank}.npy"), dvals.numpy())
+        if rank == 0:
+            np.save(os.path.join(out_dir, "C.npy"), C.numpy())
+            np.save(os.path.join(out_dir, "dB.npy"), dB.numpy())
+    finally:
+        dist.destroy_process_group()
