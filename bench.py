@@ -371,14 +371,15 @@ def extra_batched(dev, N=64, count=512, headline=None):
         mats = [api.CsrMatrix.from_host(A, dev, dt) for A in mats_h]
         Bs = [b.to(dt) for b in B32]
         target, tried = autotune.tune_batch(mats, Bs, N)
-        plan = batched.BatchedSpMM(mats, Bs, out_dtype=cdt, knobs=autotune.batch_knobs(mats, N, target))
+        strategies, knobs = autotune.batch_plan(mats, N, target)  # strategy and chunk per matrix
+        plan = batched.BatchedSpMM(mats, Bs, out_dtype=cdt, knobs=knobs, strategies=strategies)
         plan.capture()
         ms = _event_ms(plan.replay, 10, stream)
         err = []
         for i in range(0, count, 64):  # spot-check a few matrices against FP32 per-matrix results
             ref = outs[i].double()
             err.append(float((plan.out[i].double() - ref).norm() / max(float(ref.norm()), 1e-300)))
-        res[name] = {"ms": ms, "speedup_vs_plain_fp32": plain_ms / ms,
+        res[name] = {"ms": ms, "rbsr_matrices": strategies.count("rbsr"), "speedup_vs_plain_fp32": plain_ms / ms,
                      "speedup_vs_plain_fp32_graph": plain_graph_ms / ms, "chunk_target": target,
                      "max_normwise_rel_vs_fp32": max(err), "gnnz_per_s": res["nnz"] / ms / 1e6}
     # like for like: the same batch in FP32 and BF16, and BF16 per nonzero

@@ -95,9 +95,15 @@ typedef struct {
  *                    coarsen_factor; ebpr/rbpr derive it from N as the
  *                    reference does)
  *   thread_nz        staged tiles per worker step (ebsr ThreadNz)
- *   kahan_threshold  rows (segments) longer than this accumulate with
- *                    compensated summation; <= 0 selects the default
- *                    (1024), INT32_MAX disables it. */
+ *   kahan_threshold  SpMM: the nonzeros of a row longer than this are
+ *                    accumulated with compensated (Kahan) summation by the
+ *                    sequential strategies (ebsr, rbsr, and rbpr within each
+ *                    slot); ebpr adds in a shuffle-scan tree.  segment_coo
+ *                    (sequential family): a chunk longer than this is
+ *                    summed with compensation.  Partials of rows or
+ *                    segments that straddle chunks are always combined with
+ *                    compensation.  <= 0 selects the default (1024),
+ *                    INT32_MAX disables the per-row compensation. */
 typedef struct {
   int32_t group_factor;
   int32_t tile_factor;
@@ -322,6 +328,21 @@ ss_status ss_batch_plan(int count, const ss_csr *mats, int N,
                         const ss_knobs *per_mat, void *host_buf,
                         size_t host_bytes, void *dev_buf, size_t dev_bytes,
                         void *stream);
+/* The same with a strategy per matrix: per_mat_strategy[m] is SS_EBSR
+ * (element-balanced chunks, as above) or SS_RBSR (row-balanced: items are
+ * blocks of whole rows holding about one chunk of nonzeros, so every row is
+ * summed in order by one worker with no straddling rows, rbsr's arithmetic);
+ * NULL = all SS_EBSR.  The reference has no batched mode; its four
+ * strategies are separate launchers (spmm_cg.cuh:553-555, 664-666). */
+ss_status ss_batch_plan_size_ex(int count, const ss_csr *mats, int N,
+                                const ss_knobs *per_mat,
+                                const int *per_mat_strategy,
+                                size_t *host_bytes, size_t *dev_bytes);
+ss_status ss_batch_plan_ex(int count, const ss_csr *mats, int N,
+                           const void *const *B, void *const *C, int c_dtype,
+                           const ss_knobs *per_mat, const int *per_mat_strategy,
+                           void *host_buf, size_t host_bytes, void *dev_buf,
+                           size_t dev_bytes, void *stream);
 ss_status ss_spmm_batched(const void *host_plan, void *dev_plan, void *stream);
 
 #ifdef __cplusplus

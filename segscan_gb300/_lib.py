@@ -116,6 +116,11 @@ _SIGNATURES = {
                                    POINTER(c_size_t)]),
     "ss_batch_plan": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(c_void_p), POINTER(c_void_p), c_int,
                               POINTER(SsKnobs), c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
+    "ss_batch_plan_size_ex": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(SsKnobs), POINTER(c_int),
+                                      POINTER(c_size_t), POINTER(c_size_t)]),
+    "ss_batch_plan_ex": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(c_void_p), POINTER(c_void_p), c_int,
+                                 POINTER(SsKnobs), POINTER(c_int), c_void_p, c_size_t, c_void_p, c_size_t,
+                                 c_void_p]),
     "ss_spmm_batched": (c_int, [c_void_p, c_void_p, c_void_p]),
 }
 

@@ -206,13 +206,27 @@ def batch_knobs(mats, N: int, target_chunk: int = 512) -> list[SsKnobs]:
     return out
 
 
+def batch_plan(mats, N: int, target_chunk: int = 512) -> tuple[list[str], list[SsKnobs]]:
+    """(strategy, knobs) of each matrix of a batch: the knobs of batch_knobs,
+    and the strategy the single-matrix heuristic gives for its row-length
+    statistics: "rbsr" (blocks of whole rows) for short regular rows, else
+    "ebsr" (element-balanced chunks)."""
+    knobs = batch_knobs(mats, N, target_chunk)
+    strategies = []
+    for A in mats:
+        f = features(A) if A.nrow > 0 else {"cv": 0.0, "max": 0}
+        strategies.append("rbsr" if A.nnz > 0 and heuristic(f, N, A.dtype)[0] == "rbsr" else "ebsr")
+    return strategies, knobs
+
+
 def tune_batch(mats, Bs, N: int, candidates=(256, 512, 1024, 2048), iters: int = 5):
     """Measures the batched launch for each target chunk; returns
     (best target, {target: ms})."""
     from . import batched
     times = {}
     for t in candidates:
-        plan = batched.BatchedSpMM(mats, Bs, knobs=batch_knobs(mats, N, t))
+        strategies, knobs = batch_plan(mats, N, t)
+        plan = batched.BatchedSpMM(mats, Bs, knobs=knobs, strategies=strategies)
         plan.run()
         s = torch.cuda.current_stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -1,5 +1,6 @@
 // Batched SpMM host side: plan building and the launch (kernels in
 // batched.cuh, instantiated per storage type in batched_*.cu).
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -11,8 +12,10 @@ static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Fills h (everything but the offsets' final sizes) and per-matrix chunk
 // sizes; returns the number of items.
-static ss_status batch_layout(int count, const ss_csr *mats, int N, const ss_knobs *per_mat, BatchHeader &h,
-                              std::vector<BatchMat> *out) {
+// strategies: per matrix SS_EBSR (element-balanced chunks) or SS_RBSR
+// (blocks of whole rows), null = all SS_EBSR.
+static ss_status batch_layout(int count, const ss_csr *mats, int N, const ss_knobs *per_mat, const int *strategies,
+                              BatchHeader &h, std::vector<BatchMat> *out) {
   if (count < 1 || !mats || N < 1) return fail(SS_ERR_INVALID_ARG, "batch needs count >= 1, N >= 1 and matrices");
   const int dt = mats[0].value_dtype;
   ss_knobs k0;
@@ -55,6 +58,16 @@ static ss_status batch_layout(int count, const ss_csr *mats, int N, const ss_kno
     bm.nnz = A.nnz;
     bm.chunk = tnz * h.G;
     bm.num_chunks = A.nnz > 0 ? ceil_div(A.nnz, bm.chunk) : (A.nrow > 0 ? 1 : 0);
+    const int strategy = strategies ? strategies[m] : SS_EBSR;
+    if (strategy != SS_EBSR && strategy != SS_RBSR)
+      return fail(SS_ERR_UNSUPPORTED_KNOBS, "matrix %d: batched strategy %d is neither SS_EBSR nor SS_RBSR", m,
+                  strategy);
+    if (strategy == SS_RBSR && A.nnz > 0) {
+      // whole rows per item, about one chunk of nonzeros at the mean row length
+      const long long rows = ((long long)bm.chunk * A.nrow + A.nnz - 1) / A.nnz;
+      bm.rows_per_item = (int)std::min<long long>(std::max(1LL, rows), (long long)A.nrow);
+      bm.num_chunks = ceil_div(A.nrow, bm.rows_per_item);
+    }
     bm.item_begin = (int)items;
     bm.use_tma = (((uintptr_t)A.indices & 15u) == 0) && (A.values == nullptr || ((uintptr_t)A.values & 15u) == 0) &&
                  (bm.chunk % 8) == 0;
@@ -89,24 +102,24 @@ using namespace ss;
 
 extern "C" {
 
-ss_status ss_batch_plan_size(int count, const ss_csr *mats, int N, const ss_knobs *per_mat, size_t *host_bytes,
-                             size_t *dev_bytes) {
+ss_status ss_batch_plan_size_ex(int count, const ss_csr *mats, int N, const ss_knobs *per_mat,
+                                const int *per_mat_strategy, size_t *host_bytes, size_t *dev_bytes) {
   if (!host_bytes || !dev_bytes) return fail(SS_ERR_INVALID_ARG, "null size pointer");
   BatchHeader h;
-  ss_status st = batch_layout(count, mats, N, per_mat, h, nullptr);
+  ss_status st = batch_layout(count, mats, N, per_mat, per_mat_strategy, h, nullptr);
   if (st) return st;
   *host_bytes = host_bytes_for(h);
   *dev_bytes = h.dev_bytes;
   return SS_OK;
 }
 
-ss_status ss_batch_plan(int count, const ss_csr *mats, int N, const void *const *B, void *const *C, int c_dtype,
-                        const ss_knobs *per_mat, void *host_buf, size_t host_bytes, void *dev_buf, size_t dev_bytes,
-                        void *stream) {
+ss_status ss_batch_plan_ex(int count, const ss_csr *mats, int N, const void *const *B, void *const *C,
+                           int c_dtype, const ss_knobs *per_mat, const int *per_mat_strategy, void *host_buf,
+                           size_t host_bytes, void *dev_buf, size_t dev_bytes, void *stream) {
   if (!B || !C || !host_buf || !dev_buf) return fail(SS_ERR_INVALID_ARG, "null pointer");
   BatchHeader h;
   std::vector<BatchMat> bm;
-  ss_status st = batch_layout(count, mats, N, per_mat, h, &bm);
+  ss_status st = batch_layout(count, mats, N, per_mat, per_mat_strategy, h, &bm);
   if (st) return st;
   if (c_dtype != SS_F32 && c_dtype != h.val_dtype) return fail(SS_ERR_INVALID_ARG, "c_dtype must be F32 or the value dtype");
   h.c_dtype = c_dtype;
@@ -136,6 +149,18 @@ ss_status ss_batch_plan(int count, const ss_csr *mats, int N, const void *const 
     e = cudaMemcpyAsync((char *)dev_buf + h.item_mat_off, him, 4 * (size_t)h.total_items, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host buffer may be reused after return
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "batch plan upload");
+}
+
+ss_status ss_batch_plan_size(int count, const ss_csr *mats, int N, const ss_knobs *per_mat, size_t *host_bytes,
+                             size_t *dev_bytes) {
+  return ss_batch_plan_size_ex(count, mats, N, per_mat, nullptr, host_bytes, dev_bytes);
+}
+
+ss_status ss_batch_plan(int count, const ss_csr *mats, int N, const void *const *B, void *const *C, int c_dtype,
+                        const ss_knobs *per_mat, void *host_buf, size_t host_bytes, void *dev_buf, size_t dev_bytes,
+                        void *stream) {
+  return ss_batch_plan_ex(count, mats, N, B, C, c_dtype, per_mat, nullptr, host_buf, host_bytes, dev_buf, dev_bytes,
+                          stream);
 }
 
 ss_status ss_spmm_batched(const void *host_plan, void *dev_plan, void *stream) {

@@ -4,7 +4,9 @@
 // A plan (host + device copies, built by ss_batch_plan) lists the matrices
 // and numbers their work items: item i is chunk (i - item_begin[m]) of
 // matrix m = item_mat[i], a chunk being thread_nz * G consecutive nonzeros
-// of that matrix (its own knob).  The persistent kernel runs one resident
+// of that matrix (its own knob, element-balanced), or, for a matrix planned
+// row-balanced, a block of whole rows holding about that many nonzeros (each
+// row then summed in order by one group, as rbsr sums it).  The persistent kernel runs one resident
 // wave; every group takes the next item from a device counter (atomicAdd,
 // no waiting on other groups) and walks it with the ebsr chunk walk
 // (eb_walk.cuh) against that matrix's arrays.  Straddling rows go to the
@@ -24,11 +26,11 @@ struct BatchMat {
   const void *B;
   void *C;
   int M, K, nnz;
-  int chunk;        // nonzeros per item
-  int num_chunks;   // items of this matrix (1 zero-fill item when nnz == 0)
-  int item_begin;   // first item of this matrix
+  int chunk;          // element-balanced: nonzeros per item
+  int num_chunks;     // items of this matrix (1 zero-fill item when nnz == 0)
+  int item_begin;     // first item of this matrix
   int use_tma;
-  int pad;
+  int rows_per_item;  // row-balanced (> 0): whole rows per item, no row split
 };
 
 struct BatchHeader {
@@ -123,9 +125,17 @@ __global__ void __launch_bounds__(512, SS_SR_MIN_BLOCKS) batched_kernel(const ch
     a.carry_cnt = rows_all + (size_t)mt.item_begin * h.tiles;
     a.carry_vals = heads_all + (size_t)mt.item_begin * h.N;
     a.tail_vals = tails_all + (size_t)mt.item_begin * h.N;
-    const bool done = a.chunk > h.kahan
-                          ? sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm)
-                          : sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
+    int cs, ce;
+    if (mt.rows_per_item > 0) {  // a block of whole rows: each row summed by this group alone
+      const int r0 = chunk * mt.rows_per_item;
+      cs = __ldg(mt.indptr + r0);
+      ce = __ldg(mt.indptr + min(mt.M, r0 + mt.rows_per_item));
+      if (cs == ce) continue;  // empty rows only: the item holding the next nonzero zeroes them
+    } else {
+      cs = chunk * mt.chunk;
+      ce = min(cs + mt.chunk, mt.nnz);
+    }
+    const bool done = sr_spmm_chunk<T, TC, V, NV>(a, chunk, cs, ce, lane, mask, st, L, col0, act, keep, strm);
     if (!done) break;  // a bounded wait expired
   }
 }

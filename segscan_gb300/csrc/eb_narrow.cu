@@ -108,7 +108,6 @@ __global__ void __launch_bounds__(512) eb_narrow_kernel(EbArgs a) {
   for (int j = 0; j < NV; j++) act[j] = col0 + j * V < a.N;
   const uint64_t keep = policy_keep(a.keep_frac), strm = policy_stream();
   const unsigned self = 1u << (threadIdx.x & 31);
-  const bool kahan = a.chunk > a.kahan;
   // 16-byte loads of the column / value streams: chunks start on multiples
   // of 8 nonzeros, so every block of 8 is aligned when the arrays are
   const bool vec = use_vec_streams(a);
@@ -117,10 +116,12 @@ __global__ void __launch_bounds__(512) eb_narrow_kernel(EbArgs a) {
     const int cs = chunk * a.chunk;
     const int ce = min(cs + a.chunk, a.nnz);
     int r = row_search(a.indptr, 1, a.M, cs);  // row of nonzero cs
-    const bool has_head = cs > 0 && __ldg(a.indptr + r) < cs;
+    const int start = __ldg(a.indptr + r);
+    const bool has_head = cs > 0 && start < cs;
     const int head = has_head ? r : -1;
     if (cs == 0 && !a.accumulate) narrow_zero<TC, V, NV>(a, 0, r - 1, col0, act, strm);
     int end = __ldg(a.indptr + r + 1);  // one past row r's last nonzero
+    bool kahan = end - start > a.kahan;  // row r is compensated
     float acc[NV][V], comp[NV][V];
     #pragma unroll
     for (int j = 0; j < NV; j++)
@@ -159,7 +160,9 @@ __global__ void __launch_bounds__(512) eb_narrow_kernel(EbArgs a) {
             #pragma unroll
             for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
           r++;
-          end = __ldg(a.indptr + r + 1);
+          const int next = __ldg(a.indptr + r + 1);
+          kahan = next - end > a.kahan;
+          end = next;
         }
         #pragma unroll
         for (int j = 0; j < NV; j++)

@@ -18,6 +18,8 @@
 //    indptr staged in shared memory - no per-nonzero search;
 //  * four B rows are gathered ahead of the multiply-adds, with registers
 //    capped at 64 so that 32+ warps per SM keep enough gathers in flight;
+//  * rows longer than kahan_threshold accumulate with compensated
+//    summation: the tile labelling marks their nonzeros;
 //  * a row is flushed when the walk passes its end (eb_common.cuh: owner
 //    store, head/tail slots for the two rows that straddle the chunk,
 //    zeros for empty rows).
@@ -86,7 +88,9 @@ __device__ __forceinline__ void stage_issue(const EbArgs &a, Stage &st, const Sr
   const int32_t *scol = SEG ? a.index : a.cols;
   const T *sval = SEG ? nullptr : (const T *)a.vals;
   __syncwarp(mask);  // every lane is done reading buffer b
-  const bool tma = a.use_tma && (n % 8) == 0;
+  // bulk copies need 16-byte aligned sources and sizes: 8-element multiples
+  // (row-aligned batch items start anywhere; their misaligned tiles load plainly)
+  const bool tma = a.use_tma && (n % 8) == 0 && (sb % 8) == 0;
   st.tma = tma ? (st.tma | (1u << b)) : (st.tma & ~(1u << b));
   if (tma) {
     if (lane == 0) {
@@ -144,6 +148,14 @@ __device__ __forceinline__ void add_row(float (&acc)[NV][V], float (&comp)[NV][V
     }
 }
 
+// acc += v * b, compensated when the row is longer than the threshold.
+template <int V, int NV>
+__device__ __forceinline__ void add_row(float (&acc)[NV][V], float (&comp)[NV][V], float v,
+                                        const float (&b)[NV][V], bool kahan) {
+  if (kahan) add_row<V, NV, true>(acc, comp, v, b);
+  else add_row<V, NV, false>(acc, comp, v, b);
+}
+
 // ---------------------------------------------------------------------
 // SpMM chunk walk
 //
@@ -175,11 +187,16 @@ __device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)
   }
 }
 
-// Returns false when a bounded wait expired (the caller then stops).
-template <typename T, typename TC, int V, int NV, bool KAHAN>
-__device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int lane, unsigned mask, Stage &st,
-                                              const SrLayout &L, int col0, const bool (&act)[NV], uint64_t keep,
-                                              uint64_t strm) {
+// Walks nonzeros [cs, ce) as work item `chunk` (its head / tail slots).
+// Element-balanced items are chunk * a.chunk onwards; a row-balanced item
+// (batched) starts and ends on row boundaries, so no row straddles it.
+// Rows longer than a.kahan are summed with compensation (per row: the tile
+// labelling marks their nonzeros).  Returns false when a bounded wait
+// expired (the caller then stops).
+template <typename T, typename TC, int V, int NV>
+__device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs, int ce, int lane, unsigned mask,
+                                              Stage &st, const SrLayout &L, int col0, const bool (&act)[NV],
+                                              uint64_t keep, uint64_t strm) {
   const T *__restrict__ B = (const T *)a.B;
   const int G = a.team_lanes;
   const bool ones = a.vals == nullptr;
@@ -188,8 +205,8 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
   constexpr int SR_FU = V * NV >= 8 ? 2 : 4;
   constexpr int SR_UP = V * NV >= 8 ? 2 : SR_U;
   ChunkInfo ci;
-  ci.cs = chunk * a.chunk;
-  ci.ce = min(ci.cs + a.chunk, a.nnz);
+  ci.cs = cs;
+  ci.ce = ce;
   const int nst = (ci.ce - ci.cs + L.S - 1) / L.S;
   stage_issue<T, false>(a, st, L, 0, ci.cs, min(L.S, ci.ce - ci.cs), lane, G, mask, strm);
   if (nst > 1) stage_issue<T, false>(a, st, L, 1, ci.cs + L.S, min(L.S, ci.ce - ci.cs - L.S), lane, G, mask, strm);
@@ -266,15 +283,18 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
     const bool fast = st.win[L.W - 1] > last || win_base + L.W - 1 >= a.M;
 
     if (fast) {
-      // ---- label the tile's nonzeros with row | end-of-row bit; empty rows
-      // starting where a row's first nonzero sits are zeroed by the whole
-      // group (each lane owns one column slice)
+      // ---- label the tile's nonzeros with row | end-of-row bit, and mark
+      // those of rows longer than the compensation threshold (kmask bit e);
+      // empty rows starting where a row's first nonzero sits are zeroed by
+      // the whole group (each lane owns one column slice)
       const int c0 = cur - win_base;
       const int rounds = (n + G - 1) / G;
       bool bad = false;  // a column outside [0, K) in this tile
+      uint64_t kmask = 0;
       for (int k = 0; k < rounds; k++) {
         const int e = lane + k * G;
         int zlo = 0, zhi = -1;
+        bool kah = false;
         if (e < n) {
           bad |= (unsigned)scol[e] >= (unsigned)a.K;
           const int p = sb + e;
@@ -285,6 +305,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
           }
           const int rr = lo - 1;  // window slot of p's row
           const bool end = st.win[rr + 1] == p + 1;
+          kah = st.win[rr + 1] - st.win[rr] > a.kahan;
           sinfo[e] = (win_base + rr) | (end ? (int)0x80000000 : 0);
           if (st.win[rr] == p && p != ci.cs) {  // p opens row rr: empties before it start at p too
             int q = rr - 1;
@@ -293,6 +314,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
             zhi = win_base + rr - 1;
           }
         }
+        kmask |= (uint64_t)group_ballot(mask, kah, G) << (k * G);
         unsigned todo = __ballot_sync(mask, zlo <= zhi);
         while (todo) {
           const int src = __ffs(todo) - 1;
@@ -306,8 +328,8 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
       // a full tile of valid columns takes the lean loop: four staged
       // columns, labels and values per shared-memory read, no bounds checks
       const bool full = n == L.S && !__any_sync(mask, bad);
-      auto consume = [&](int info, float v, const float (&b)[NV][V]) {
-        add_row<V, NV, KAHAN>(acc, comp, v, b);
+      auto consume = [&](int info, float v, const float (&b)[NV][V], bool kah) {
+        add_row<V, NV>(acc, comp, v, b, kah);
         cur = info & 0x7fffffff;
         open = true;
         if (info < 0) {
@@ -319,6 +341,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
         const int4 *col4 = reinterpret_cast<const int4 *>(scol);
         const int4 *info4 = reinterpret_cast<const int4 *>(sinfo);
         for (int q = 0; q < n; q += 4) {
+          const unsigned k4 = (unsigned)(kmask >> q) & 0xfu;  // compensated nonzeros among these four
           const int4 cc = col4[q >> 2];
           const int4 in4 = info4[q >> 2];
           const int cs4[4] = {cc.x, cc.y, cc.z, cc.w};
@@ -349,7 +372,11 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
                 }
               }
             #pragma unroll
-            for (int u = 0; u < SR_FU; u++) consume(is4[h + u], v4[h + u], bv[u]);
+            for (int u = 0; u < SR_FU; u++) {
+              // long rows are rare: the plain path unless one of these is in one
+              if (k4 == 0) consume(is4[h + u], v4[h + u], bv[u], false);
+              else consume(is4[h + u], v4[h + u], bv[u], (k4 >> (h + u)) & 1u);
+            }
           }
         }
       } else for (int q = 0; q < n; q += SR_UP) {  // ---- partial tile: gather, multiply, store at row ends
@@ -371,7 +398,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
         #pragma unroll
         for (int u = 0; u < SR_UP; u++) {
           if (q + u >= n) break;
-          consume(sinfo[q + u], ones ? 1.f : Elem<T>::to_f(sval[q + u]), bv[u]);
+          consume(sinfo[q + u], ones ? 1.f : Elem<T>::to_f(sval[q + u]), bv[u], (kmask >> (q + u)) & 1u);
         }
       }
     } else {
@@ -386,6 +413,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
           if (next_start <= sb && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
         }
       }
+      bool kah = next_start - wget(cur) > a.kahan;  // row cur is compensated
       for (int q = 0; q < n; q++) {
         const int p = sb + q;
         const int c = scol[q];
@@ -408,9 +436,10 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int la
             if (ns <= p && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
           } while (ns <= p && cur < a.M - 1);
           next_start = ns;
+          kah = next_start - wget(cur) > a.kahan;
         }
         const float v = ones ? 1.f : Elem<T>::to_f(sval[q]);
-        add_row<V, NV, KAHAN>(acc, comp, v, bq);
+        add_row<V, NV>(acc, comp, v, bq, kah);
         open = true;
       }
       // close a row that ends exactly at the tile end; the next tile zeroes
@@ -585,7 +614,7 @@ __global__ void __launch_bounds__(512, SS_SR_MIN_BLOCKS) eb_sr_kernel(EbArgs a) 
   #pragma unroll
   for (int j = 0; j < NV; j++) act[j] = col0 + j * V < a.N;
   const uint64_t keep = policy_keep(a.keep_frac), strm = policy_stream();
-  const bool kahan = a.chunk > a.kahan;
+  const bool kahan = a.chunk > a.kahan;  // segments: compensated within a chunk longer than the threshold
   const int stride = gridDim.x * a.workers_per_block;
   for (int chunk = blockIdx.x * a.workers_per_block + wib; chunk < a.num_chunks; chunk += stride) {
     bool ok;
@@ -593,8 +622,9 @@ __global__ void __launch_bounds__(512, SS_SR_MIN_BLOCKS) eb_sr_kernel(EbArgs a) 
       ok = kahan ? sr_seg_chunk<T, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, strm)
                  : sr_seg_chunk<T, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, strm);
     } else {
-      ok = kahan ? sr_spmm_chunk<T, TC, V, NV, true>(a, chunk, lane, mask, st, L, col0, act, keep, strm)
-                 : sr_spmm_chunk<T, TC, V, NV, false>(a, chunk, lane, mask, st, L, col0, act, keep, strm);
+      const int cs = chunk * a.chunk;
+      ok = sr_spmm_chunk<T, TC, V, NV>(a, chunk, cs, min(cs + a.chunk, a.nnz), lane, mask, st, L, col0, act,
+                                       keep, strm);
     }
     // a bounded wait expired: the group waited again for its copies in
     // flight and issues nothing more into its buffers

@@ -71,3 +71,35 @@ def test_batched_equals_per_matrix(cuda):
     torch.cuda.synchronize()
     for a, b in zip(plan.out, outs):  # same chunks, same order: identical bits
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_batched_row_balanced_items(cuda, dtype):
+    """Matrices planned row-balanced (items are blocks of whole rows) next to
+    element-balanced ones in one launch: every output within 1e-5 of FP64,
+    and each row-balanced output bit-identical to the single-matrix rbsr
+    launch (one group sums each row in order, as rbsr does), including a row
+    above the compensation threshold and matrices with empty rows."""
+    from segscan_gb300 import api, autotune, batched
+    N = 64
+    host = small_batch(12, seed=9)
+    host += [synth.poisson(3000, 2000, 9.0, seed=4), synth.banded(5000, 5000, 20, 100, seed=2),
+             synth.poisson(1, 3000, 2500.0, seed=6), synth.poisson(4000, 1000, 0.3, seed=7)]
+    mats = [dev_csr(A, dtype) for A in host]
+    Bh = [synth.dense(A.ncol, N, seed=40 + i) for i, A in enumerate(host)]
+    Bs = [torch.from_numpy(B).cuda().to(dtype) for B in Bh]
+    strategies, knobs = autotune.batch_plan(mats, N, 256)
+    strategies = ["rbsr" if i % 2 or i >= 12 else s for i, s in enumerate(strategies)]  # plenty of both kinds
+    plan = batched.BatchedSpMM(mats, Bs, knobs=knobs, strategies=strategies)
+    plan.out = [o.fill_(float("nan")) for o in plan.out]
+    plan.run()
+    torch.cuda.synchronize()
+    for i, A in enumerate(host):
+        vals = rounded(A.values, dtype) if dtype != torch.float32 else A.values
+        C64, absC = oracle64(A, rounded(Bh[i], dtype), vals)
+        check_close(plan.out[i].cpu().numpy(), C64, absC, 1e-5, None, f"matrix {i} ({strategies[i]}) {dtype}")
+        if strategies[i] == "rbsr" and A.nnz > 0:
+            single = api.spmm(mats[i], Bs[i], "rbsr", knobs=api.make_knobs("rbsr", N, coarsen_factor=4,
+                                                                           tile_factor=6))
+            torch.cuda.synchronize()
+            assert torch.equal(plan.out[i], single), f"matrix {i}: row-balanced item differs from rbsr"
