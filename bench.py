@@ -478,8 +478,9 @@ def extra_sweep(A_pl, dev):
 def extra_fwd_bwd(dev, N=128):
     """Differentiated SpMM layer: power-law 2e6 x 2e6 (Zipf 2.1 clipped to
     [1, 50000], seed 4), B 2e6 x 128, dC ~ N(0, 1).  Forward C = A B;
-    backward dA.vals = SDDMM(dC, B), dB = A^T dC on the device-built
-    transpose (built once per pattern; its time is reported apart)."""
+    backward dA.vals and dB = A^T dC from one fused walk over the
+    device-built transpose (built once per pattern; its time is reported
+    apart), with the separate SDDMM and A^T dC times beside it."""
     import numpy as np
     import torch
     from segscan_gb300 import api, autograd, synth
@@ -520,8 +521,12 @@ def extra_fwd_bwd(dev, N=128):
         AT_v = AT.with_values(api.gather_values(vals.detach().float(), perm))
         dB = torch.empty((A.ncol, N), device=dev)
         db = _event_ms(lambda: api.spmm(AT_v, dC, "ebsr", knobs=knobs32, out=dB), 5, stream)
-        return {"fwd_bwd_ms": total, "fwd_ms": f, "bwd_ms": total - f, "sddmm_ms": sd, "dB_spmm_ms": db,
-                "transpose_build_ms": t_ms, "knobs_fwd": knobs.as_dict()}
+        # the backward the autograd binding runs: both gradients from one walk over A^T
+        out16 = dt if dt != torch.float32 else None
+        fb = _event_ms(lambda: api.spmm_backward(AT, perm, vals.detach(), dC, Bd.detach(), out16), 5, stream)
+        return {"fwd_bwd_ms": total, "fwd_ms": f, "bwd_ms": total - f, "fused_bwd_ms": fb,
+                "separate_sddmm_ms": sd, "separate_dB_spmm_ms": db, "transpose_build_ms": t_ms,
+                "knobs_fwd": knobs.as_dict()}
 
     # each precision in its own scope, the allocator's cache emptied between,
     # so one run's gigabyte-sized temporaries do not crowd the next

@@ -274,6 +274,26 @@ ss_status ss_gather_values(const void *values, int dtype, const int32_t *perm,
 ss_status ss_sddmm(const ss_csr *A, int N, const float *dC, const void *B,
                    float *dvals, void *stream);
 
+/* Fused backward of C = A*B, walked over the rows of A^T: dB = A^T * dC and
+ * dvals[p] = dot(dC[i, :], B[k, :]) at every stored nonzero p = (i, k), one
+ * gather of each dC row serving both (ss_sddmm followed by an SpMM on A^T
+ * gathers a B row and then a dC row per nonzero).  AT is the pattern of A^T
+ * as ss_csr_transpose builds it (nrow = A's ncol, ncol = A's nrow; its
+ * values are not read; value_dtype = the storage type of `values` and B);
+ * perm [nnz] maps an A^T position to its A position.  values: A's values in
+ * A's order (NULL = ones).  dC [A.nrow x N] FP32; B [A.ncol x N] of
+ * value_dtype; dB [A.ncol x N] SS_F32 or value_dtype, overwritten, each row
+ * summed in position order (compensated above kahan_threshold, <= 0 = 1024)
+ * as rbsr sums A^T's rows; dvals [nnz] FP32 in A's order.  A group of lanes
+ * owns a row of A^T, so a very long row of A^T (a dense column of A) is one
+ * group's work.  N up to 64 x the widest vector of <= 4 FP32 dividing N
+ * (256 for N divisible by 4); beyond that SS_ERR_UNSUPPORTED_KNOBS (use
+ * ss_sddmm and ss_spmm on A^T).  No counterpart in the reference. */
+ss_status ss_spmm_backward(const ss_csr *AT, const int32_t *perm,
+                           const void *values, int N, const float *dC,
+                           const void *B, void *dB, int dB_dtype,
+                           float *dvals, int kahan_threshold, void *stream);
+
 /* Checks indptr (0 first, nnz last, monotone) and column range; writes 0 to
  * *d_flag (device int) when A is well formed, else a nonzero code. */
 ss_status ss_csr_validate(const ss_csr *A, int32_t *d_flag, void *stream);

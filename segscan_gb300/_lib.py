@@ -110,6 +110,8 @@ _SIGNATURES = {
                                  c_void_p]),
     "ss_gather_values": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
     "ss_sddmm": (c_int, [POINTER(SsCsr), c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ss_spmm_backward": (c_int, [POINTER(SsCsr), c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int,
+                                 c_void_p, c_int, c_void_p]),
     "ss_csr_validate": (c_int, [POINTER(SsCsr), c_void_p, c_void_p]),
     "ss_index_validate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p]),
     "ss_batch_plan_size": (c_int, [c_int, POINTER(SsCsr), c_int, POINTER(SsKnobs), POINTER(c_size_t),

@@ -562,3 +562,40 @@ def sddmm(A: CsrMatrix, dC: torch.Tensor, B: torch.Tensor, stream=None) -> torch
     d = A.descr()
     _lib.call("ss_sddmm", ctypes.byref(d), int(B.shape[1]), _ptr(dC), _ptr(B), _ptr(out), _stream(stream))
     return out
+
+
+def spmm_backward_limit(N: int) -> int:
+    """Largest N the fused backward covers at this width's vector size."""
+    V = 4
+    while V > 1 and N % V:
+        V //= 2
+    return 64 * V
+
+
+@_allocates_on_launch_stream
+def spmm_backward(AT: CsrMatrix, perm: torch.Tensor, values: Optional[torch.Tensor], dC: torch.Tensor,
+                  B: torch.Tensor, out_dtype: Optional[torch.dtype] = None, kahan_threshold: int = 0,
+                  stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+    """(dvals, dB) of C = A @ B from one walk over A^T's rows (AT, perm from
+    transpose(A)): dvals[p] = dot(dC[i, :], B[k, :]) in A's order, FP32, and
+    dB = A^T @ dC in out_dtype (FP32 by default, or B's dtype)."""
+    _need_cuda("dC", dC, torch.float32)
+    _need_cuda("B", B)
+    _need_cuda("perm", perm, torch.int32)
+    if values is not None:
+        _need_cuda("values", values, B.dtype)
+        if values.numel() != AT.nnz:
+            raise ValueError(f"values ({values.numel()}) and A^T ({AT.nnz}) differ in nonzeros")
+    N = int(B.shape[1])
+    if dC.shape != (AT.ncol, N) or B.shape[0] != AT.nrow:
+        raise ValueError(f"dC must be [{AT.ncol}, N] and B [{AT.nrow}, N]")
+    if perm.numel() != AT.nnz:
+        raise ValueError(f"perm ({perm.numel()}) and A^T ({AT.nnz}) differ in nonzeros")
+    cdt = out_dtype or torch.float32
+    dB = _output((AT.nrow, N), cdt, dC.device)
+    dvals = _output(AT.nnz, torch.float32, dC.device)
+    d = AT.with_values(None).descr()
+    d.value_dtype = int(dtype_code(B.dtype))
+    _lib.call("ss_spmm_backward", ctypes.byref(d), _ptr(perm), _ptr(values), N, _ptr(dC), _ptr(B), _ptr(dB),
+              int(dtype_code(cdt)), _ptr(dvals), int(kahan_threshold), _stream(stream))
+    return dvals, dB

@@ -3,11 +3,13 @@
 Forward: C = A @ B with one of the four strategies.  It saves only the
 sparse pattern, A's values and B; nothing is recomputed in backward.
 Backward:
+  both gradients wanted: one fused walk over A^T's rows
+  (ss_spmm_backward), each dC row gathered once for dB[k] += a * dC[i]
+  and dA.vals[p] = dot(dC[i], B[k]); A^T's pattern is built on the device
+  by the stable counting-sort transpose once per pattern and cached;
+  one of them, or N above the fused walk's width:
   dA.vals = SDDMM(dC, B)            (ss_sddmm: dot of dC row i with B row k)
-  dB      = A^T @ dC                (the forward kernels on A^T, whose
-                                     pattern is built on the device by the
-                                     stable counting-sort transpose once per
-                                     pattern and cached)
+  dB      = A^T @ dC                (the forward kernels on A^T)
 Values stored in BF16/FP16 get FP32 gradients cast back to their dtype;
 dB is computed in FP32 (A^T values widened to FP32) and rounded to B's dtype
 by the ebsr walk's own stores (other strategies: a cast after).
@@ -52,6 +54,15 @@ class SpMMFunction(torch.autograd.Function):
         pattern: _Pattern = ctx.pattern
         dC = dC.contiguous().float()
         d_values = d_B = None
+        if ctx.needs_input_grad[0] and ctx.needs_input_grad[1] and B.shape[1] <= api.spmm_backward_limit(
+                int(B.shape[1])):
+            # both gradients from one walk over A^T: each dC row gathered once
+            AT, perm = pattern.transposed()
+            out_dtype = B.dtype if B.dtype != torch.float32 else None
+            knobs = ctx.bw_knobs
+            d_values, d_B = api.spmm_backward(AT, perm, values.contiguous(), dC, B.contiguous(), out_dtype,
+                                              knobs.kahan_threshold if knobs is not None else 0)
+            return d_values.to(values.dtype), d_B.to(B.dtype), None, None, None, None, None
         if ctx.needs_input_grad[0]:
             A = pattern.A.with_values(values)
             d_values = api.sddmm(A, dC, B.contiguous()).to(values.dtype)

@@ -1,0 +1,183 @@
+// Fused backward of C = A * B, walked over the rows of A^T.
+//
+// No counterpart in the reference (it has no backward).  For a row k of A^T
+// (a column of A) and each of its nonzeros q = (k, i), whose position in A
+// is p = perm[q] and value a = values[p]:
+//   dB[k, :]  = sum over the row's q, in order, of a * dC[i, :]
+//   dvals[p]  = dot(dC[i, :], B[k, :])
+// so one gather of the dC row serves both gradients: SDDMM followed by
+// A^T * dC would gather a B row and then a dC row for every nonzero.
+//
+// A group of L lanes along N owns a row of A^T (lane l holds elements
+// (j * L + l) * V .. + V - 1 for j < NV, so each gathered row is one
+// contiguous request per j), keeps that row of B in registers, and walks
+// the row's nonzeros four at a time with their four dC rows in flight.
+// The four partial dot products are reduced across the lanes by a fixed
+// butterfly (butterfly_sum); dB is summed in position order, with Kahan
+// compensation when the row is longer than the threshold, so dB has the
+// bits of the row-balanced sequential SpMM (rbsr) on A^T.  FP32 math.
+#include "common.cuh"
+#include "internal.h"
+
+namespace ss {
+
+constexpr int BWD_U = 4;  // nonzeros (dC rows) in flight per group
+
+struct BwdArgs {
+  int K, M, N, nnz, kahan;
+  const int32_t *t_indptr, *t_indices, *perm;
+  const void *vals;  // A's values in A's order, or null (ones)
+  const float *dC;   // [M x N]
+  const void *B;     // [K x N], the values' storage type
+  void *dB;          // [K x N]
+  float *dvals;      // [nnz], A's order
+  int lanes, log2_lanes;
+};
+
+template <typename T, typename TC, int V, int NV>
+__global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
+  const int tid = threadIdx.x;
+  const int L = a.lanes;
+  const int lane = tid & (L - 1);
+  const int group = (blockIdx.x * blockDim.x + tid) >> a.log2_lanes;
+  const int groups = (gridDim.x * blockDim.x) >> a.log2_lanes;
+  const unsigned wl = tid & 31;
+  const unsigned mask = L >= 32 ? 0xffffffffu : (((1u << L) - 1u) << (wl & ~(unsigned)(L - 1)));
+  const uint64_t keep = policy_keep(1.0f), strm = policy_stream();
+  const T *B = (const T *)a.B;
+  const T *vals = (const T *)a.vals;
+  bool act[NV];
+  #pragma unroll
+  for (int j = 0; j < NV; j++) act[j] = (j * L + lane) * V < a.N;
+  for (int k = group; k < a.K; k += groups) {
+    const int s = __ldg(a.t_indptr + k), e = __ldg(a.t_indptr + k + 1);
+    const bool kahan = e - s > a.kahan;
+    float b[NV][V], acc[NV][V], comp[NV][V];
+    #pragma unroll
+    for (int j = 0; j < NV; j++) {
+      #pragma unroll
+      for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; b[j][i] = 0.f; }
+      if (act[j] && e > s) load_vec<T, V>(B + (int64_t)k * a.N + (j * L + lane) * V, b[j], strm);
+    }
+    for (int q0 = s; q0 < e; q0 += BWD_U) {
+      int row[BWD_U], pos[BWD_U];
+      float av[BWD_U];
+      float g[BWD_U][NV][V];
+      #pragma unroll
+      for (int u = 0; u < BWD_U; u++) {
+        const bool live = q0 + u < e;
+        row[u] = live ? ld_idx(a.t_indices + q0 + u, strm) : -1;
+        pos[u] = live ? ld_idx(a.perm + q0 + u, strm) : -1;
+      }
+      #pragma unroll
+      for (int u = 0; u < BWD_U; u++) {
+        const bool ok = (unsigned)row[u] < (unsigned)a.M && (unsigned)pos[u] < (unsigned)a.nnz;
+        av[u] = ok ? load_val<T>(vals, pos[u], keep) : 0.f;
+        #pragma unroll
+        for (int j = 0; j < NV; j++) {
+          if (ok && act[j]) {
+            load_vec<float, V>(a.dC + (int64_t)row[u] * a.N + (j * L + lane) * V, g[u][j], keep);
+          } else {
+            #pragma unroll
+            for (int i = 0; i < V; i++) g[u][j][i] = 0.f;
+          }
+        }
+      }
+      float part[BWD_U];
+      #pragma unroll
+      for (int u = 0; u < BWD_U; u++) {
+        part[u] = 0.f;
+        #pragma unroll
+        for (int j = 0; j < NV; j++)
+          #pragma unroll
+          for (int i = 0; i < V; i++) {
+            part[u] = fmaf(g[u][j][i], b[j][i], part[u]);
+            if (kahan) kahan_add(acc[j][i], comp[j][i], av[u] * g[u][j][i]);
+            else acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
+          }
+      }
+      // the four dot products: reduced across the lanes, stored at A's positions
+      if (L >= BWD_U) {
+        int base = 0;
+        const float x = butterfly_sum<BWD_U>(part, lane, L, mask, base);
+        if ((lane & (L / BWD_U - 1)) == 0 && pos[base] >= 0 && pos[base] < a.nnz) a.dvals[pos[base]] = x;
+      } else {
+        #pragma unroll
+        for (int u = 0; u < BWD_U; u++) {
+          float x = part[u];
+          for (int off = L >> 1; off > 0; off >>= 1) x += __shfl_xor_sync(mask, x, off);
+          if (lane == 0 && pos[u] >= 0 && pos[u] < a.nnz) a.dvals[pos[u]] = x;
+        }
+      }
+    }
+    TC *dst = (TC *)a.dB + (int64_t)k * a.N;
+    #pragma unroll
+    for (int j = 0; j < NV; j++)
+      if (act[j]) store_vec<TC, V>(dst + (j * L + lane) * V, acc[j], strm);
+  }
+}
+
+template <typename T, typename TC>
+static void *bwd_ptr(int V, int NV) {
+  if (NV == 1) {
+    if (V == 1) return (void *)fused_bwd_kernel<T, TC, 1, 1>;
+    if (V == 2) return (void *)fused_bwd_kernel<T, TC, 2, 1>;
+    if (V == 4) return (void *)fused_bwd_kernel<T, TC, 4, 1>;
+  } else {
+    if (V == 1) return (void *)fused_bwd_kernel<T, TC, 1, 2>;
+    if (V == 2) return (void *)fused_bwd_kernel<T, TC, 2, 2>;
+    if (V == 4) return (void *)fused_bwd_kernel<T, TC, 4, 2>;
+  }
+  return nullptr;
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" ss_status ss_spmm_backward(const ss_csr *AT, const int32_t *perm, const void *values, int N,
+                                      const float *dC, const void *B, void *dB, int dB_dtype, float *dvals,
+                                      int kahan_threshold, void *stream) {
+  ss::NvtxRange nvtx_range("ss_spmm_backward");
+  if (!AT || AT->nrow < 0 || AT->ncol < 0 || AT->nnz < 0 || N < 0) return fail(SS_ERR_INVALID_ARG, "bad arguments");
+  const int dt = AT->value_dtype;
+  if (dt < SS_F32 || dt > SS_F16) return fail(SS_ERR_INVALID_ARG, "value_dtype %d unknown", dt);
+  if (dB_dtype != SS_F32 && dB_dtype != dt) return fail(SS_ERR_INVALID_ARG, "dB_dtype must be SS_F32 or the value dtype");
+  const int K = AT->nrow, M = AT->ncol, nnz = AT->nnz;
+  if (K == 0 || N == 0) return SS_OK;
+  if (!AT->indptr || !dB || (nnz > 0 && (!AT->indices || !perm || !dC || !B || !dvals)))
+    return fail(SS_ERR_INVALID_ARG, "null pointer");
+  // V: widest vector (<= 16 bytes of FP32 dC) dividing N; lanes and NV cover N
+  int V = 4;
+  while (V > 1 && (N % V) != 0) V >>= 1;
+  int lanes = ceil_pow2(ceil_div(N, V));
+  if (lanes > 32) lanes = 32;
+  const int NV = ceil_div(N, lanes * V);
+  if (NV > 2)
+    return fail(SS_ERR_UNSUPPORTED_KNOBS, "fused backward covers N <= %d here (got %d); use ss_sddmm and ss_spmm on A^T",
+                64 * V, N);
+  const int es = dtype_size(dt), cs = dtype_size(dB_dtype);
+  if (((uintptr_t)dC % (4 * V)) || ((uintptr_t)B % (es * V)) || ((uintptr_t)dB % (cs * V)) ||
+      ((uintptr_t)values % es) || ((uintptr_t)perm % 4))
+    return fail(SS_ERR_ALIGNMENT, "dC / B / dB not aligned to the %d-element vector access", V);
+  void *fn = nullptr;
+  if (dt == SS_F32) fn = bwd_ptr<float, float>(V, NV);
+  else if (dt == SS_BF16) fn = dB_dtype == SS_F32 ? bwd_ptr<__nv_bfloat16, float>(V, NV)
+                                                  : bwd_ptr<__nv_bfloat16, __nv_bfloat16>(V, NV);
+  else fn = dB_dtype == SS_F32 ? bwd_ptr<__half, float>(V, NV) : bwd_ptr<__half, __half>(V, NV);
+  if (!fn) return fail(SS_ERR_UNSUPPORTED_KNOBS, "no fused backward kernel for V=%d NV=%d", V, NV);
+  BwdArgs a;
+  a.K = K; a.M = M; a.N = N; a.nnz = nnz;
+  a.kahan = kahan_threshold > 0 ? kahan_threshold : 1024;
+  a.t_indptr = AT->indptr; a.t_indices = AT->indices; a.perm = perm; a.vals = values;
+  a.dC = dC; a.B = B; a.dB = dB; a.dvals = dvals;
+  a.lanes = lanes; a.log2_lanes = ilog2(lanes);
+  const int threads = 256;
+  const long long groups_per_block = threads / lanes;
+  long long blocks = ((long long)K + groups_per_block - 1) / groups_per_block;
+  const long long cap = (long long)sm_count() * 8;
+  if (blocks > cap) blocks = cap;
+  void *args[] = {&a};
+  cudaError_t e = cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, 0, (cudaStream_t)stream);
+  return e == cudaSuccess ? SS_OK : cuda_fail(e, "fused backward launch");
+}

@@ -257,6 +257,35 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
   return ok != 0;
 }
 
+// Sums U per-lane partials across `lanes` lanes (lanes >= U, powers of two):
+// a reduce-scatter butterfly halves the set of values at each of the top
+// log2(U) lane bits (U - 1 shuffles), then each lane's one remaining value
+// is summed over the lower bits.  Returns that sum; `base` gets the index
+// (in [0, U)) of the value this lane holds.  Lanes whose low log2(lanes / U)
+// bits are zero hold finished sums, one per index.  The order of the
+// additions is fixed, so results are reproducible bit for bit.
+template <int U>
+__device__ __forceinline__ float butterfly_sum(float (&v)[U], int lane, int lanes, unsigned mask, int &base) {
+  base = 0;
+  int h = lanes >> 1;
+  #pragma unroll
+  for (int cnt = U; cnt > 1; cnt >>= 1) {
+    const int half = cnt >> 1;
+    const bool hi = lane & h;
+    #pragma unroll
+    for (int i = 0; i < half; i++) {
+      const float keep = hi ? v[i + half] : v[i];
+      const float send = hi ? v[i] : v[i + half];
+      v[i] = keep + __shfl_xor_sync(mask, send, h);
+    }
+    base += hi ? half : 0;
+    h >>= 1;
+  }
+  float x = v[0];
+  for (int off = h; off > 0; off >>= 1) x += __shfl_xor_sync(mask, x, off);
+  return x;
+}
+
 // Compensated (Kahan) accumulation step: acc += x with running error c.
 __device__ __forceinline__ void kahan_add(float &acc, float &c, float x) {
   float y = x - c;

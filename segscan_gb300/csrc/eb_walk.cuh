@@ -19,7 +19,12 @@
 //  * four B rows are gathered ahead of the multiply-adds, with registers
 //    capped at 64 so that 32+ warps per SM keep enough gathers in flight;
 //  * rows longer than kahan_threshold accumulate with compensated
-//    summation: the tile labelling marks their nonzeros;
+//    summation: the tile labelling marks their nonzeros.  In full tiles,
+//    four consecutive nonzeros of such a row are summed plainly and the
+//    four-term sum is added with one compensated step (the few beside a row
+//    end are added plainly), so the rounding error is that of four-term
+//    blocks plus the compensated sum, whatever the row's length; other
+//    tiles compensate every nonzero of such a row;
 //  * a row is flushed when the walk passes its end (eb_common.cuh: owner
 //    store, head/tail slots for the two rows that straddle the chunk,
 //    zeros for empty rows).
@@ -29,6 +34,8 @@
 // issues no more.  This header holds the kernel templates; eb_walk_*.cu
 // instantiate them per storage type and eb_walk.cu launches them.
 #pragma once
+#include <type_traits>
+
 #include "eb_common.cuh"
 #include "internal.h"
 
@@ -337,11 +344,13 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
           open = false;
         }
       };
-      if (full) {
+      // the full-tile loop, without (LONG false) or with the compensated
+      // four-term blocks of long rows; most tiles hold no long row
+      auto full_tile = [&](auto long_tag) {
+        constexpr bool LONG = decltype(long_tag)::value;
         const int4 *col4 = reinterpret_cast<const int4 *>(scol);
         const int4 *info4 = reinterpret_cast<const int4 *>(sinfo);
         for (int q = 0; q < n; q += 4) {
-          const unsigned k4 = (unsigned)(kmask >> q) & 0xfu;  // compensated nonzeros among these four
           const int4 cc = col4[q >> 2];
           const int4 in4 = info4[q >> 2];
           const int cs4[4] = {cc.x, cc.y, cc.z, cc.w};
@@ -357,6 +366,12 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
             unpack2(x.x, v4[0], v4[1], (T *)nullptr);
             unpack2(x.y, v4[2], v4[3], (T *)nullptr);
           }
+          // four nonzeros inside one long row (no row end among the first
+          // three): summed with plain FMAs, and the block sum added to the row
+          // with one compensated step, so the rounding error stays that of a
+          // four-term block whatever the row's length
+          const bool block = LONG && ((unsigned)(kmask >> q) & 0xfu) == 0xfu && (in4.x | in4.y | in4.z) >= 0;
+          float blk[NV][V];
           #pragma unroll
           for (int h = 0; h < 4; h += SR_FU) {
             float bv[SR_FU][NV][V];
@@ -373,12 +388,34 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
               }
             #pragma unroll
             for (int u = 0; u < SR_FU; u++) {
-              // long rows are rare: the plain path unless one of these is in one
-              if (k4 == 0) consume(is4[h + u], v4[h + u], bv[u], false);
-              else consume(is4[h + u], v4[h + u], bv[u], (k4 >> (h + u)) & 1u);
+              if (LONG && block) {
+                #pragma unroll
+                for (int j = 0; j < NV; j++)
+                  #pragma unroll
+                  for (int i = 0; i < V; i++)
+                    blk[j][i] = h + u == 0 ? v4[0] * bv[u][j][i] : fmaf(v4[h + u], bv[u][j][i], blk[j][i]);
+              } else {  // short rows, and a long row's nonzeros beside a row end: plain sums
+                consume(is4[h + u], v4[h + u], bv[u], false);
+              }
+            }
+          }
+          if (LONG && block) {
+            #pragma unroll
+            for (int j = 0; j < NV; j++)
+              #pragma unroll
+              for (int i = 0; i < V; i++) kahan_add(acc[j][i], comp[j][i], blk[j][i]);
+            cur = in4.w & 0x7fffffff;
+            open = true;
+            if (in4.w < 0) {
+              flush_done(cur);
+              open = false;
             }
           }
         }
+      };
+      if (full) {
+        if (kmask) full_tile(std::true_type{});
+        else full_tile(std::false_type{});
       } else for (int q = 0; q < n; q += SR_UP) {  // ---- partial tile: gather, multiply, store at row ends
         float bv[SR_UP][NV][V];
         #pragma unroll

@@ -15,31 +15,13 @@ namespace ss {
 constexpr int SDDMM_CHUNK = 128;  // nonzeros per team chunk
 constexpr int SDDMM_U = 8;  // nonzeros per step
 
-// Sums U per-lane partials across `lanes` lanes (lanes >= U, powers of two)
-// and stores the U dot products: a reduce-scatter butterfly halves the set
-// of values at each of the top log2(U) lane bits (U - 1 shuffles), then each
-// lane's one remaining value is summed over the lower bits; lanes whose low
-// bits are zero hold a finished sum, of nonzero `base`.
+// Stores the U dot products reduced by butterfly_sum (common.cuh): the
+// lanes holding a finished sum write it, to nonzero p0 + its index.
 template <int U>
 __device__ __forceinline__ void butterfly_store(float (&v)[U], int lane, int lanes, unsigned mask, float *out,
                                                 int p0, int ce) {
   int base = 0;
-  int h = lanes >> 1;
-  #pragma unroll
-  for (int cnt = U; cnt > 1; cnt >>= 1) {
-    const int half = cnt >> 1;
-    const bool hi = lane & h;
-    #pragma unroll
-    for (int i = 0; i < half; i++) {
-      const float keep = hi ? v[i + half] : v[i];
-      const float send = hi ? v[i] : v[i + half];
-      v[i] = keep + __shfl_xor_sync(mask, send, h);
-    }
-    base += hi ? half : 0;
-    h >>= 1;
-  }
-  float x = v[0];
-  for (int off = h; off > 0; off >>= 1) x += __shfl_xor_sync(mask, x, off);
+  const float x = butterfly_sum<U>(v, lane, lanes, mask, base);
   if ((lane & (lanes / U - 1)) == 0 && p0 + base < ce) out[p0 + base] = x;
 }
 

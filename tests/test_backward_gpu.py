@@ -194,3 +194,48 @@ def test_coo_to_csr(cuda, case):
     assert np.array_equal(perm.cpu().numpy()[:m], order)
     assert np.array_equal(A.indices.cpu().numpy()[:m], cols[order])
     assert np.array_equal(A.values.cpu().numpy()[:m], vals[order])
+
+
+@pytest.mark.parametrize("N", [1, 3, 8, 64, 128, 256])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("which", ["powerlaw", "long_columns"])
+def test_fused_backward(cuda, N, dtype, which):
+    """ss_spmm_backward against FP64: dB = A^T dC and dvals = SDDMM(dC, B)
+    within 1e-5 of sum|terms| (on the values and B the kernel reads); for
+    FP32, dB bit-identical to rbsr on A^T with the gathered values (both sum
+    each row of A^T in position order)."""
+    from segscan_gb300 import api
+    csr = powerlaw_medium() if which == "powerlaw" else long_column_matrix()
+    A = dev_csr(csr, dtype)
+    B = synth.dense(csr.ncol, N, seed=N + 3)
+    dC = synth.dense(csr.nrow, N, seed=N + 4)
+    Bd = torch.from_numpy(B).cuda().to(dtype)
+    dCd = torch.from_numpy(dC).cuda()
+    AT, perm = api.transpose(A)
+    dvals, dB = api.spmm_backward(AT, perm, A.values, dCd, Bd)
+    torch.cuda.synchronize()
+    vals = rounded(csr.values, dtype) if dtype != torch.float32 else csr.values
+    Bh = rounded(B, dtype) if dtype != torch.float32 else B
+    t_indptr, t_indices, operm = oracle_lib.csr_transpose(csr.indptr, csr.indices, csr.ncol)
+    dB64, dBabs = oracle_lib.spmm_f64(t_indptr, t_indices, vals[operm], dC)
+    dv64, dvabs = oracle_lib.sddmm_f64(csr.indptr, csr.indices, dC, Bh)
+    check_close(dB.cpu().numpy(), dB64, dBabs, 1e-5, 1e-5, f"fused dB {which} N={N} {dtype}")
+    check_close(dvals.cpu().numpy(), dv64, dvabs, 1e-5, 1e-5, f"fused dvals {which} N={N} {dtype}")
+    if dtype == torch.float32:
+        AT_v = AT.with_values(api.gather_values(A.values, perm))
+        ref = api.spmm(AT_v, dCd, "rbsr", knobs=api.make_knobs("rbsr", N, coarsen_factor=4, tile_factor=7))
+        torch.cuda.synchronize()
+        assert torch.equal(dB, ref), f"fused dB differs from rbsr on A^T ({which}, N={N})"
+
+
+def test_fused_backward_wide_refused(cuda):
+    """N above the fused walk's width is refused before any launch."""
+    from segscan_gb300 import api
+    from segscan_gb300._lib import SegscanError
+    csr = synth.poisson(100, 80, 3.0, seed=1)
+    A = dev_csr(csr)
+    AT, perm = api.transpose(A)
+    N = 260
+    with pytest.raises(SegscanError):
+        api.spmm_backward(AT, perm, A.values, torch.zeros((100, N), device="cuda"),
+                          torch.zeros((80, N), device="cuda"))
