@@ -249,6 +249,15 @@ ss_status ss_csr_transpose_workspace_size(const ss_csr *A, size_t *bytes);
 ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr,
                            int32_t *t_indices, int32_t *perm, void *ws,
                            size_t ws_bytes, void *stream);
+/* As ss_csr_transpose, and t_values [nnz] = A's values in transposed order
+ * (A->value_dtype; the same as ss_gather_values on perm, in the same pass).
+ * t_values NULL: the pattern only.  Same workspace.  Entries past
+ * t_indptr[ncol] (nonzeros whose column is outside [0, ncol)) get perm and
+ * t_indices -1. */
+ss_status ss_csr_transpose_values(const ss_csr *A, int32_t *t_indptr,
+                                  int32_t *t_indices, int32_t *perm,
+                                  void *t_values, void *ws, size_t ws_bytes,
+                                  void *stream);
 
 /* COO -> CSR on the device, the counterpart of compressedRow
  * (test-cg/include/dataloader/dataloader.hpp:109-121), which assumes its

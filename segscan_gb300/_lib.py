@@ -108,6 +108,8 @@ _SIGNATURES = {
     "ss_csr_transpose_workspace_size": (c_int, [POINTER(SsCsr), POINTER(c_size_t)]),
     "ss_csr_transpose": (c_int, [POINTER(SsCsr), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                  c_void_p]),
+    "ss_csr_transpose_values": (c_int, [POINTER(SsCsr), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_size_t, c_void_p]),
     "ss_gather_values": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
     "ss_sddmm": (c_int, [POINTER(SsCsr), c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "ss_spmm_backward": (c_int, [POINTER(SsCsr), c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int,

@@ -495,7 +495,8 @@ def segment_coo_sorted_sr(src, index, nnz, N, dst, *, CoarsenFactor, ThreadNz, D
 @_allocates_on_launch_stream
 def transpose(A: CsrMatrix, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
     """(A^T pattern with values gathered, perm): stable counting-sort transpose
-    on the device (dataloader.hpp:109-144); perm[q] = source nonzero of entry q."""
+    on the device (dataloader.hpp:109-144); perm[q] = source nonzero of entry q.
+    The values are gathered in the same pass (ss_csr_transpose_values)."""
     d = A.descr()
     dev = A.indptr.device
     n = ctypes.c_size_t()
@@ -505,11 +506,9 @@ def transpose(A: CsrMatrix, stream=None) -> tuple[CsrMatrix, torch.Tensor]:
     t_indptr = _output(A.ncol + 1, torch.int32, dev)
     t_indices = _output(A.nnz, torch.int32, dev)
     perm = _output(A.nnz, torch.int32, dev)
-    _lib.call("ss_csr_transpose", ctypes.byref(d), _ptr(t_indptr), _ptr(t_indices), _ptr(perm), wp, wn,
-              _stream(stream))
-    vals = None
-    if A.values is not None:
-        vals = gather_values(A.values, perm, stream)
+    vals = _output(A.values.shape, A.values.dtype, dev) if A.values is not None else None
+    _lib.call("ss_csr_transpose_values", ctypes.byref(d), _ptr(t_indptr), _ptr(t_indices), _ptr(perm),
+              _ptr(vals), wp, wn, _stream(stream))
     return CsrMatrix(A.ncol, A.nrow, t_indptr, t_indices, vals), perm
 
 

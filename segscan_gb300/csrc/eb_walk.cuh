@@ -19,12 +19,9 @@
 //  * four B rows are gathered ahead of the multiply-adds, with registers
 //    capped at 64 so that 32+ warps per SM keep enough gathers in flight;
 //  * rows longer than kahan_threshold accumulate with compensated
-//    summation: the tile labelling marks their nonzeros.  In full tiles,
-//    four consecutive nonzeros of such a row are summed plainly and the
-//    four-term sum is added with one compensated step (the few beside a row
-//    end are added plainly), so the rounding error is that of four-term
-//    blocks plus the compensated sum, whatever the row's length; other
-//    tiles compensate every nonzero of such a row;
+//    summation, every nonzero of them: a chunk that touches such a row (read
+//    off the staged indptr window) takes the walk whose tile labelling marks
+//    their nonzeros; other chunks take a walk without compensation terms;
 //  * a row is flushed when the walk passes its end (eb_common.cuh: owner
 //    store, head/tail slots for the two rows that straddle the chunk,
 //    zeros for empty rows).
@@ -34,7 +31,6 @@
 // issues no more.  This header holds the kernel templates; eb_walk_*.cu
 // instantiate them per storage type and eb_walk.cu launches them.
 #pragma once
-#include <type_traits>
 
 #include "eb_common.cuh"
 #include "internal.h"
@@ -194,16 +190,37 @@ __device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)
   }
 }
 
-// Walks nonzeros [cs, ce) as work item `chunk` (its head / tail slots).
-// Element-balanced items are chunk * a.chunk onwards; a row-balanced item
-// (batched) starts and ends on row boundaries, so no row straddles it.
-// Rows longer than a.kahan are summed with compensation (per row: the tile
-// labelling marks their nonzeros).  Returns false when a bounded wait
-// expired (the caller then stops).
-template <typename T, typename TC, int V, int NV>
-__device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs, int ce, int lane, unsigned mask,
-                                              Stage &st, const SrLayout &L, int col0, const bool (&act)[NV],
-                                              uint64_t keep, uint64_t strm) {
+// True when a row with more than a.kahan nonzeros overlaps [cs, ce).  The
+// window holds indptr from win_base on, win_base being the row that holds
+// cs or an earlier one; every row it covers is checked.  When the chunk
+// runs past the window, the rows wholly inside the chunk are no longer than
+// the chunk, so only the row holding ce - 1 is left to look up (a chunk
+// longer than the threshold is then taken as holding a long row).
+__device__ __forceinline__ bool chunk_has_long_row(const EbArgs &a, const Stage &st, const SrLayout &L, int cs,
+                                                   int ce, int lane, int G, unsigned mask) {
+  bool found = false;
+  for (int i = lane; i < L.W - 1; i += G) {
+    const int s = st.win[i], e = st.win[i + 1];
+    found |= s < ce && e > cs && e - s > a.kahan;
+  }
+  found = __any_sync(mask, found);
+  if (found || st.win[L.W - 1] >= ce) return found;  // entries past row M hold nnz
+  if (ce - cs > a.kahan) return true;
+  const int r = group_lower_bound(a.indptr, a.M, ce, lane, G, mask);  // row r - 1 holds ce - 1
+  return __ldg(a.indptr + r) - __ldg(a.indptr + r - 1) > a.kahan;
+}
+
+// Walks nonzeros [cs, ce) as work item `chunk` (its head / tail slots); the
+// first two tiles are in flight, lb is the first row starting at or after
+// cs and the window holds indptr from win_base on.  KAH: some row of the
+// chunk is longer than a.kahan; the tile labelling then marks the nonzeros
+// of such rows, which are summed with compensation.  Without KAH the walk
+// carries no compensation terms at all, which keeps it within its register
+// budget.  Returns false when a bounded wait expired (the caller then stops).
+template <typename T, typename TC, int V, int NV, bool KAH>
+__device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs, int ce, int nst, int lb,
+                                             int win_base, int lane, unsigned mask, Stage &st, const SrLayout &L,
+                                             int col0, const bool (&act)[NV], uint64_t keep, uint64_t strm) {
   const T *__restrict__ B = (const T *)a.B;
   const int G = a.team_lanes;
   const bool ones = a.vals == nullptr;
@@ -214,13 +231,6 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
   ChunkInfo ci;
   ci.cs = cs;
   ci.ce = ce;
-  const int nst = (ci.ce - ci.cs + L.S - 1) / L.S;
-  stage_issue<T, false>(a, st, L, 0, ci.cs, min(L.S, ci.ce - ci.cs), lane, G, mask, strm);
-  if (nst > 1) stage_issue<T, false>(a, st, L, 1, ci.cs + L.S, min(L.S, ci.ce - ci.cs - L.S), lane, G, mask, strm);
-
-  // first row: lb = first row starting at or after cs
-  const int lb = group_lower_bound(a.indptr, a.M, ci.cs, lane, G, mask);
-  int win_base = lb;
   auto win_fill = [&](int base) {
     __syncwarp(mask);
     win_base = base;
@@ -231,7 +241,6 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
     if (r - win_base >= L.W || r < win_base) win_fill(r);
     return st.win[r - win_base];
   };
-  win_fill(lb);
   int cur;
   ci.has_head = lb > 0 && wget(lb) > ci.cs;  // cs lies inside row lb - 1
   if (ci.has_head) {
@@ -290,10 +299,10 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
     const bool fast = st.win[L.W - 1] > last || win_base + L.W - 1 >= a.M;
 
     if (fast) {
-      // ---- label the tile's nonzeros with row | end-of-row bit, and mark
-      // those of rows longer than the compensation threshold (kmask bit e);
-      // empty rows starting where a row's first nonzero sits are zeroed by
-      // the whole group (each lane owns one column slice)
+      // ---- label the tile's nonzeros with row | end-of-row bit (and, with
+      // KAH, mark those of long rows: kmask bit e); empty rows starting where
+      // a row's first nonzero sits are zeroed by the whole group (each lane
+      // owns one column slice)
       const int c0 = cur - win_base;
       const int rounds = (n + G - 1) / G;
       bool bad = false;  // a column outside [0, K) in this tile
@@ -312,7 +321,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
           }
           const int rr = lo - 1;  // window slot of p's row
           const bool end = st.win[rr + 1] == p + 1;
-          kah = st.win[rr + 1] - st.win[rr] > a.kahan;
+          if (KAH) kah = st.win[rr + 1] - st.win[rr] > a.kahan;
           sinfo[e] = (win_base + rr) | (end ? (int)0x80000000 : 0);
           if (st.win[rr] == p && p != ci.cs) {  // p opens row rr: empties before it start at p too
             int q = rr - 1;
@@ -321,7 +330,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
             zhi = win_base + rr - 1;
           }
         }
-        kmask |= (uint64_t)group_ballot(mask, kah, G) << (k * G);
+        if (KAH) kmask |= (uint64_t)group_ballot(mask, kah, G) << (k * G);
         unsigned todo = __ballot_sync(mask, zlo <= zhi);
         while (todo) {
           const int src = __ffs(todo) - 1;
@@ -336,7 +345,8 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
       // columns, labels and values per shared-memory read, no bounds checks
       const bool full = n == L.S && !__any_sync(mask, bad);
       auto consume = [&](int info, float v, const float (&b)[NV][V], bool kah) {
-        add_row<V, NV>(acc, comp, v, b, kah);
+        if (KAH) add_row<V, NV>(acc, comp, v, b, kah);
+        else add_row<V, NV, false>(acc, comp, v, b);
         cur = info & 0x7fffffff;
         open = true;
         if (info < 0) {
@@ -344,10 +354,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
           open = false;
         }
       };
-      // the full-tile loop, without (LONG false) or with the compensated
-      // four-term blocks of long rows; most tiles hold no long row
-      auto full_tile = [&](auto long_tag) {
-        constexpr bool LONG = decltype(long_tag)::value;
+      if (full) {
         const int4 *col4 = reinterpret_cast<const int4 *>(scol);
         const int4 *info4 = reinterpret_cast<const int4 *>(sinfo);
         for (int q = 0; q < n; q += 4) {
@@ -366,12 +373,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
             unpack2(x.x, v4[0], v4[1], (T *)nullptr);
             unpack2(x.y, v4[2], v4[3], (T *)nullptr);
           }
-          // four nonzeros inside one long row (no row end among the first
-          // three): summed with plain FMAs, and the block sum added to the row
-          // with one compensated step, so the rounding error stays that of a
-          // four-term block whatever the row's length
-          const bool block = LONG && ((unsigned)(kmask >> q) & 0xfu) == 0xfu && (in4.x | in4.y | in4.z) >= 0;
-          float blk[NV][V];
+          const unsigned k4 = KAH ? (unsigned)(kmask >> q) & 0xfu : 0u;  // compensated among these four
           #pragma unroll
           for (int h = 0; h < 4; h += SR_FU) {
             float bv[SR_FU][NV][V];
@@ -387,35 +389,9 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
                 }
               }
             #pragma unroll
-            for (int u = 0; u < SR_FU; u++) {
-              if (LONG && block) {
-                #pragma unroll
-                for (int j = 0; j < NV; j++)
-                  #pragma unroll
-                  for (int i = 0; i < V; i++)
-                    blk[j][i] = h + u == 0 ? v4[0] * bv[u][j][i] : fmaf(v4[h + u], bv[u][j][i], blk[j][i]);
-              } else {  // short rows, and a long row's nonzeros beside a row end: plain sums
-                consume(is4[h + u], v4[h + u], bv[u], false);
-              }
-            }
-          }
-          if (LONG && block) {
-            #pragma unroll
-            for (int j = 0; j < NV; j++)
-              #pragma unroll
-              for (int i = 0; i < V; i++) kahan_add(acc[j][i], comp[j][i], blk[j][i]);
-            cur = in4.w & 0x7fffffff;
-            open = true;
-            if (in4.w < 0) {
-              flush_done(cur);
-              open = false;
-            }
+            for (int u = 0; u < SR_FU; u++) consume(is4[h + u], v4[h + u], bv[u], (k4 >> (h + u)) & 1u);
           }
         }
-      };
-      if (full) {
-        if (kmask) full_tile(std::true_type{});
-        else full_tile(std::false_type{});
       } else for (int q = 0; q < n; q += SR_UP) {  // ---- partial tile: gather, multiply, store at row ends
         float bv[SR_UP][NV][V];
         #pragma unroll
@@ -450,7 +426,7 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
           if (next_start <= sb && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
         }
       }
-      bool kah = next_start - wget(cur) > a.kahan;  // row cur is compensated
+      bool kah = KAH && next_start - wget(cur) > a.kahan;  // row cur is compensated
       for (int q = 0; q < n; q++) {
         const int p = sb + q;
         const int c = scol[q];
@@ -473,10 +449,11 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
             if (ns <= p && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
           } while (ns <= p && cur < a.M - 1);
           next_start = ns;
-          kah = next_start - wget(cur) > a.kahan;
+          kah = KAH && next_start - wget(cur) > a.kahan;
         }
         const float v = ones ? 1.f : Elem<T>::to_f(sval[q]);
-        add_row<V, NV>(acc, comp, v, bq, kah);
+        if (KAH) add_row<V, NV>(acc, comp, v, bq, kah);
+        else add_row<V, NV, false>(acc, comp, v, bq);
         open = true;
       }
       // close a row that ends exactly at the tile end; the next tile zeroes
@@ -504,6 +481,34 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
   if (head >= 0) carry_arrive<TC, V, NV>(a, head, lane, G, mask, col0, act, strm);
   if (tail) carry_arrive<TC, V, NV>(a, cur, lane, G, mask, col0, act, strm);
   return true;
+}
+
+// Walks nonzeros [cs, ce) as work item `chunk`.  Element-balanced items are
+// chunk * a.chunk onwards; a row-balanced item (batched) starts and ends on
+// row boundaries, so no row straddles it.  The first two tiles are issued,
+// the first row searched and the indptr window filled from the row holding
+// cs; the walk is then the compensated one only when the chunk touches a row
+// longer than a.kahan.  Returns false when a bounded wait expired.
+template <typename T, typename TC, int V, int NV>
+__device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs, int ce, int lane, unsigned mask,
+                                              Stage &st, const SrLayout &L, int col0, const bool (&act)[NV],
+                                              uint64_t keep, uint64_t strm) {
+  const int G = a.team_lanes;
+  const int nst = (ce - cs + L.S - 1) / L.S;
+  stage_issue<T, false>(a, st, L, 0, cs, min(L.S, ce - cs), lane, G, mask, strm);
+  if (nst > 1) stage_issue<T, false>(a, st, L, 1, cs + L.S, min(L.S, ce - cs - L.S), lane, G, mask, strm);
+  // lb = first row starting at or after cs; the window starts at the row
+  // before it, which holds cs when the chunk starts inside a row
+  const int lb = group_lower_bound(a.indptr, a.M, cs, lane, G, mask);
+  const int base = lb > 0 ? lb - 1 : 0;
+  __syncwarp(mask);
+  for (int i = lane; i < L.W; i += G) st.win[i] = __ldg(a.indptr + min(base + i, a.M));
+  __syncwarp(mask);
+  if (chunk_has_long_row(a, st, L, cs, ce, lane, G, mask))
+    return sr_spmm_walk<T, TC, V, NV, true>(a, chunk, cs, ce, nst, lb, base, lane, mask, st, L, col0, act, keep,
+                                            strm);
+  return sr_spmm_walk<T, TC, V, NV, false>(a, chunk, cs, ce, nst, lb, base, lane, mask, st, L, col0, act, keep,
+                                           strm);
 }
 
 // ---------------------------------------------------------------------

@@ -1,20 +1,44 @@
-// Device CSR transpose (the backward pass's A^T) and value gather.
+// Device CSR transpose (the backward pass's A^T), value gather and COO ->
+// CSR.
 //
 // Reference semantics: transpose + compressedRow
 // (test-cg/include/dataloader/dataloader.hpp:109-144), a stable counting
 // sort by column: entries of one column keep A's CSR order.  The device
-// version gives the same result bit for bit:
-//   1. column histogram (atomics)            -> counts
+// versions give the same result bit for bit, as a sort of the nonzero
+// positions p by column with p ascending inside a column.
+//
+// ss_csr_transpose: two-level bucket sort.  A bucket is F = 2^f consecutive
+// columns, F chosen so that an average bucket fills at most half of one
+// block's shared-memory record store.
+//   1. bucket_count_kernel: per-block shared-memory histogram of col >> f,
+//      one global add per bucket per block;
+//   2. bucket_scan_kernel (one block): bucket starts, cursors, t_indptr[K];
+//   3. bucket_partition_kernel: a tile of TB_E nonzeros finds the row of
+//      each nonzero (the rows starting inside the tile are marked in shared
+//      memory and a block max-scan spreads them), reserves one range per
+//      bucket it touches and writes (position, row, column) records there;
+//   4. bucket_sort_kernel: a block per bucket counts its columns in shared
+//      memory (writing t_indptr), places the records by column and sorts
+//      each column by position (insertion sort up to 32 entries, bitonic
+//      beyond), then writes perm, t_indices and, optionally, the gathered
+//      values.  Rows grow with positions, so a column's rows sorted on their
+//      own equal the rows of its sorted positions.  A bucket larger than the
+//      record store is placed and sorted in the output arrays instead.
+// Order inside a column before step 4's sort depends on atomics; after it,
+// only on the input, so repeated calls agree.
+//
+// ss_coo_to_csr (and ss_csr_transpose beyond TB_NB_MAX buckets of 8192
+// columns): a one-level counting sort,
+//   1. key histogram (atomics)               -> counts
 //   2. exclusive scan of counts (3 kernels; 5 when K > 4096^2, the tile
 //      sums then scanned in two levels)      -> t_indptr
-//   3. scatter nonzero ids by column (atomic cursors; order inside a column
-//      is arbitrary here)                    -> perm
-//   4. sort each column's ids ascending      -> the stable order
-//      (thread insertion sort <= 32 entries, block bitonic sort in shared
-//      memory <= 16384, block bitonic sort in global memory beyond)
-//   5. t_indices[q] = row of perm[q]
-// Every step is deterministic given the input, so repeated calls agree.
+//   3. scatter positions by key (atomic cursors)
+//   4. sort each key's positions ascending (thread insertion sort <= 32
+//      entries, block bitonic sort in shared memory <= 16384, in global
+//      memory beyond)
+//   5. for the transpose: t_indices[q] = row of perm[q].
 #include <algorithm>
+#include <climits>
 
 #include "common.cuh"
 #include "internal.h"
@@ -305,6 +329,450 @@ static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "counting sort launch");
 }
 
+// ---------------------------------------------------------------------
+// Two-level bucket transpose (ss_csr_transpose)
+// ---------------------------------------------------------------------
+constexpr int TB_T = 1024;           // threads per block (partition and sort)
+constexpr int TB_PER = 8;            // nonzeros per thread in a partition tile
+constexpr int TB_E = TB_T * TB_PER;  // nonzeros per partition tile
+constexpr int TB_F_LOG2_MAX = 13;  // at most 8192 columns per bucket
+constexpr int TB_NB_MAX = 8192;    // buckets
+#ifndef SS_TB_SORT_SMEM_KB
+#define SS_TB_SORT_SMEM_KB 220
+#endif
+constexpr int TB_SORT_SMEM = SS_TB_SORT_SMEM_KB * 1024;
+constexpr int TB_LONG = 40;  // slot of the long-column count in the sort block's scratch
+
+struct BucketPlan {
+  bool ok;             // false: more than TB_NB_MAX buckets of 8192 columns
+  int f, F, NB, cap;   // F = 2^f columns per bucket; cap = records a sort block holds
+};
+
+// Records a sort block holds beside its 2F + 1 counters and 64 ints of scratch.
+static int sort_cap(int F) { return (TB_SORT_SMEM - (2 * F + 1 + 64) * 4) / 8; }
+
+static BucketPlan bucket_plan(int K, int nnz) {
+  BucketPlan p;
+  const double avg = K > 0 ? (double)nnz / K : 0.0;
+  int f = TB_F_LOG2_MAX;
+  while (f > 0 && (double)(1 << f) * avg > sort_cap(1 << f) / 2) f--;
+  long long nb = ((long long)K + (1LL << f) - 1) >> f;
+  while (nb > TB_NB_MAX && f < TB_F_LOG2_MAX) {
+    f++;
+    nb = ((long long)K + (1LL << f) - 1) >> f;
+  }
+  p.ok = nb <= TB_NB_MAX;
+  p.f = f;
+  p.F = 1 << f;
+  p.NB = (int)nb;
+  p.cap = sort_cap(p.F);
+  return p;
+}
+
+struct BucketWs {
+  int32_t *count;   // [NB]: nonzeros per bucket
+  int32_t *start;   // [NB + 1]: bucket starts
+  int32_t *cursor;  // [NB]: partition cursors
+  int32_t *pos, *row, *col;  // [nnz] records, grouped by bucket
+};
+
+static size_t bucket_ws_bytes(const BucketPlan &p, int nnz, BucketWs *w, void *base) {
+  size_t o = 0;
+  const size_t count = o; o += align256((size_t)(p.NB + 1) * 4);
+  const size_t start = o; o += align256((size_t)(p.NB + 1) * 4);
+  const size_t cursor = o; o += align256((size_t)(p.NB + 1) * 4);
+  const size_t pos = o; o += align256((size_t)nnz * 4);
+  const size_t row = o; o += align256((size_t)nnz * 4);
+  const size_t col = o; o += align256((size_t)nnz * 4);
+  if (w) {
+    char *b = (char *)base;
+    w->count = (int32_t *)(b + count);
+    w->start = (int32_t *)(b + start);
+    w->cursor = (int32_t *)(b + cursor);
+    w->pos = (int32_t *)(b + pos);
+    w->row = (int32_t *)(b + row);
+    w->col = (int32_t *)(b + col);
+  }
+  return o;
+}
+
+// Scan of x[0, n) in place by the whole block, each thread owning a
+// contiguous run of ceil(n / blockDim.x) entries: exclusive prefix sums
+// (MAX false) or inclusive prefix maxima (MAX true).  Returns the sum / the
+// maximum to every thread.  wbuf: 33 ints of shared memory.
+template <bool MAX>
+__device__ int block_scan(int32_t *x, int n, int32_t *wbuf) {
+  constexpr int ID = MAX ? INT_MIN : 0;
+  auto op = [](int u, int v) { return MAX ? max(u, v) : u + v; };
+  const int T = blockDim.x, tid = threadIdx.x;
+  const int per = (n + T - 1) / T;
+  const int lo = min(tid * per, n), hi = min(lo + per, n);
+  int t = ID;
+  for (int i = lo; i < hi; i++) t = op(t, x[i]);
+  const int lane = tid & 31, wid = tid >> 5;
+  int incl = t;
+  #pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl = op(incl, y);
+  }
+  int excl = __shfl_up_sync(0xffffffffu, incl, 1);
+  if (lane == 0) excl = ID;
+  if (lane == 31) wbuf[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    const int w = lane < (T >> 5) ? wbuf[lane] : ID;
+    int wi = w;
+    #pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, wi, off);
+      if (lane >= off) wi = op(wi, y);
+    }
+    int we = __shfl_up_sync(0xffffffffu, wi, 1);
+    if (lane == 0) we = ID;
+    wbuf[lane] = we;  // exclusive prefix of the warp totals
+    if (lane == 31) wbuf[32] = wi;
+  }
+  __syncthreads();
+  int run = op(wbuf[wid], excl);
+  for (int i = lo; i < hi; i++) {
+    const int v = x[i];
+    if (MAX) {
+      run = max(run, v);
+      x[i] = run;
+    } else {
+      x[i] = run;
+      run += v;
+    }
+  }
+  const int total = wbuf[32];
+  __syncthreads();
+  return total;
+}
+
+// Largest r in [0, M) with indptr[r] <= key (indptr[0] = 0 <= key): the 32
+// lanes of a warp probe 32 split points of the open range per round.
+__device__ int warp_row_of(const int32_t *__restrict__ indptr, int M, int key, int lane) {
+  int lo = 0, hi = M - 1;  // indptr[lo] <= key; the answer lies in [lo, hi]
+  while (lo < hi) {
+    const int probe = lo + 1 + (int)(((long long)(hi - lo) * lane) >> 5);  // in (lo, hi]
+    const bool ok = __ldg(indptr + probe) <= key;
+    const unsigned hits = __ballot_sync(0xffffffffu, ok);
+    if (!hits) {
+      hi = lo;
+      break;
+    }
+    const int last = 31 - __clz(hits);  // probes are ordered, so hits are a prefix
+    const int nlo = __shfl_sync(0xffffffffu, probe, last);
+    const int nxt = __shfl_sync(0xffffffffu, probe, last < 31 ? last + 1 : 31);
+    hi = last < 31 ? nxt - 1 : hi;
+    lo = nlo;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(TB_T) bucket_count_kernel(const int32_t *__restrict__ cols, int nnz, int K, int f,
+                                                            int NB, int32_t *count) {
+  extern __shared__ int32_t hist[];
+  for (int i = threadIdx.x; i < NB; i += TB_T) hist[i] = 0;
+  __syncthreads();
+  const long long step = (long long)gridDim.x * TB_T * 4;
+  for (long long b = (long long)blockIdx.x * TB_T * 4 + threadIdx.x; b < nnz; b += step) {
+    int c[4];
+    #pragma unroll
+    for (int u = 0; u < 4; u++) c[u] = b + u * TB_T < nnz ? __ldg(cols + b + u * TB_T) : -1;
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+      if ((unsigned)c[u] < (unsigned)K) atomicAdd(hist + (c[u] >> f), 1);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < NB; i += TB_T) {
+    const int h = hist[i];
+    if (h) atomicAdd(count + i, h);
+  }
+}
+
+// Bucket starts and partition cursors; t_indptr[K] = nonzeros with a column
+// in [0, K); the entries past it (nonzeros with other columns) get -1.
+__global__ void __launch_bounds__(TB_T) bucket_scan_kernel(const int32_t *__restrict__ count, int NB, int nnz, int K,
+                                                           int32_t *start, int32_t *cursor, int32_t *t_indptr,
+                                                           int32_t *perm, int32_t *t_indices) {
+  __shared__ int32_t x[TB_NB_MAX];
+  __shared__ int32_t wbuf[33];
+  for (int i = threadIdx.x; i < NB; i += TB_T) x[i] = count[i];
+  __syncthreads();
+  const int total = block_scan<false>(x, NB, wbuf);
+  for (int i = threadIdx.x; i < NB; i += TB_T) {
+    start[i] = x[i];
+    cursor[i] = x[i];
+  }
+  if (threadIdx.x == 0) {
+    start[NB] = total;
+    t_indptr[K] = total;
+  }
+  for (int q = total + threadIdx.x; q < nnz; q += TB_T) {
+    perm[q] = -1;
+    t_indices[q] = -1;
+  }
+}
+
+struct PartArgs {
+  const int32_t *indptr, *cols;
+  int M, K, nnz, f, NB;
+  int32_t *cursor, *pos, *row, *col;
+};
+
+// One tile of TB_E nonzeros per round: rows, then (position, row, column)
+// records into the tile's reserved range of each bucket.
+__global__ void __launch_bounds__(TB_T) bucket_partition_kernel(PartArgs a) {
+  extern __shared__ int32_t sm[];
+  int32_t *hist = sm;             // [NB]
+  int32_t *base = hist + a.NB;    // [NB]
+  int32_t *rows = base + a.NB;    // [TB_E]
+  __shared__ int32_t wbuf[33];
+  __shared__ int32_t r01[2];
+  const int tid = threadIdx.x;
+  for (long long t = blockIdx.x; t * TB_E < a.nnz; t += gridDim.x) {
+    const int b0 = (int)(t * TB_E);
+    const int n = (int)min((long long)TB_E, (long long)a.nnz - b0);
+    if (tid < 64) {  // warp 0: the row holding b0; warp 1: the row holding the tile's last nonzero
+      const int r = warp_row_of(a.indptr, a.M, tid < 32 ? b0 : b0 + n - 1, tid & 31);
+      if ((tid & 31) == 0) r01[tid >> 5] = r;
+    }
+    for (int i = tid; i < a.NB; i += TB_T) hist[i] = 0;
+    int c[TB_PER], rr[TB_PER];
+    #pragma unroll
+    for (int k = 0; k < TB_PER; k++) {
+      const int e = tid + k * TB_T;
+      c[k] = e < n ? __ldg(a.cols + b0 + e) : -1;
+    }
+    __syncthreads();
+    const int r0 = r01[0], r1 = r01[1];
+    if ((long long)(r1 - r0) <= 4LL * TB_E) {
+      // mark each row's first nonzero (the last of the rows that start
+      // there: rows before it are empty), then a running maximum
+      for (int e = tid; e < TB_E; e += TB_T) rows[e] = e == 0 ? r0 : -1;
+      __syncthreads();
+      for (int r = r0 + 1 + tid; r <= r1; r += TB_T) {
+        const int e = __ldg(a.indptr + r) - b0;
+        if ((unsigned)e < (unsigned)TB_E) atomicMax(rows + e, r);
+      }
+      __syncthreads();
+      block_scan<true>(rows, n, wbuf);
+      #pragma unroll
+      for (int k = 0; k < TB_PER; k++) {
+        const int e = tid + k * TB_T;
+        rr[k] = e < n ? rows[e] : -1;
+      }
+    } else {
+      // long runs of empty rows: a binary search in [r0, r1] per nonzero
+      #pragma unroll
+      for (int k = 0; k < TB_PER; k++) {
+        const int e = tid + k * TB_T;
+        int lo = r0, hi = r1;
+        while (lo < hi) {
+          const int mid = lo + ((hi - lo + 1) >> 1);
+          if (__ldg(a.indptr + mid) <= b0 + e) lo = mid; else hi = mid - 1;
+        }
+        rr[k] = lo;
+      }
+    }
+    #pragma unroll
+    for (int k = 0; k < TB_PER; k++)
+      if ((unsigned)c[k] < (unsigned)a.K) atomicAdd(hist + (c[k] >> a.f), 1);
+    __syncthreads();
+    for (int i = tid; i < a.NB; i += TB_T) {
+      const int h = hist[i];
+      base[i] = h ? atomicAdd(a.cursor + i, h) : 0;
+      hist[i] = 0;
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int k = 0; k < TB_PER; k++) {
+      if ((unsigned)c[k] < (unsigned)a.K) {
+        const int bk = c[k] >> a.f;
+        const int q = base[bk] + atomicAdd(hist + bk, 1);
+        a.pos[q] = b0 + tid + k * TB_T;
+        a.row[q] = rr[k];
+        a.col[q] = c[k];
+      }
+    }
+    __syncthreads();  // the next tile reuses hist, base and rows
+  }
+}
+
+// Sorts n keys ascending, the values moved along (n small).
+__device__ __forceinline__ void insertion_sort2(int32_t *k, int32_t *v, int n) {
+  for (int i = 1; i < n; i++) {
+    const int32_t x = k[i], y = v[i];
+    int j = i - 1;
+    while (j >= 0 && k[j] > x) {
+      k[j + 1] = k[j];
+      v[j + 1] = v[j];
+      j--;
+    }
+    k[j + 1] = x;
+    v[j + 1] = y;
+  }
+}
+
+// Block sort of n keys in global memory: staged through shared memory when
+// they fit.
+__device__ void sort_segment(int32_t *seg, int n, int32_t *stage, int cap) {
+  if (n <= cap) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) stage[i] = seg[i];
+    __syncthreads();
+    bitonic_block(stage, n);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) seg[i] = stage[i];
+  } else {
+    bitonic_block(seg, n);
+  }
+  __syncthreads();
+}
+
+struct SortArgs {
+  const int32_t *start, *pos, *row, *col;
+  int K, NB, f, F, cap;
+  int32_t *t_indptr, *perm, *t_indices;
+  const void *vals;  // A's values, or null: no value gather
+  void *t_vals;
+  int vsize;         // 4 or 2 bytes
+};
+
+__global__ void __launch_bounds__(TB_T, 1) bucket_sort_kernel(SortArgs a) {
+  extern __shared__ int32_t sm[];
+  int32_t *cnt = sm;                 // [F + 1]: counts, then column starts
+  int32_t *cur = cnt + a.F + 1;      // [F]: placement cursors, then the long columns
+  int32_t *wbuf = cur + a.F;         // [64]: scan scratch; [TB_LONG]: long-column count
+  int32_t *sp = wbuf + 64;           // [cap] positions
+  int32_t *sr = sp + a.cap;          // [cap] rows
+  const int tid = threadIdx.x;
+  for (int b = blockIdx.x; b < a.NB; b += gridDim.x) {
+    const int c0 = b << a.f;
+    const int nf = min(a.F, a.K - c0);
+    const int s0 = __ldg(a.start + b), n = __ldg(a.start + b + 1) - s0;
+    for (int i = tid; i < nf; i += TB_T) cnt[i] = 0;
+    if (tid == 0) wbuf[TB_LONG] = 0;
+    __syncthreads();
+    for (int i0 = 0; i0 < n; i0 += 4 * TB_T) {
+      int c[4];
+      #pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int i = i0 + tid + u * TB_T;
+        c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
+      }
+      #pragma unroll
+      for (int u = 0; u < 4; u++)
+        if ((unsigned)c[u] < (unsigned)nf) atomicAdd(cnt + c[u], 1);
+    }
+    __syncthreads();
+    const int total = block_scan<false>(cnt, nf, wbuf);
+    for (int i = tid; i < nf; i += TB_T) {
+      a.t_indptr[c0 + i] = s0 + cnt[i];
+      cur[i] = cnt[i];
+    }
+    if (tid == 0) cnt[nf] = total;
+    __syncthreads();
+    // place the records by column: in shared memory, or straight into the
+    // outputs when the bucket is larger than the record store
+    const bool fits = n <= a.cap;
+    int32_t *dp = fits ? sp : a.perm + s0;
+    int32_t *dr = fits ? sr : a.t_indices + s0;
+    for (int i0 = 0; i0 < n; i0 += 2 * TB_T) {
+      int c[2], p[2], r[2];
+      #pragma unroll
+      for (int u = 0; u < 2; u++) {
+        const int i = i0 + tid + u * TB_T;
+        c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
+        p[u] = i < n ? __ldg(a.pos + s0 + i) : 0;
+        r[u] = i < n ? __ldg(a.row + s0 + i) : 0;
+      }
+      #pragma unroll
+      for (int u = 0; u < 2; u++) {
+        if ((unsigned)c[u] < (unsigned)nf) {
+          const int q = atomicAdd(cur + c[u], 1);
+          dp[q] = p[u];
+          dr[q] = r[u];
+        }
+      }
+    }
+    __syncthreads();
+    // each column by position: short ones by a thread, long ones by the block
+    for (int i = tid; i < nf; i += TB_T) {
+      const int s = cnt[i], len = cnt[i + 1] - s;
+      if (len > 32) cur[atomicAdd(wbuf + TB_LONG, 1)] = i;
+      else if (len > 1) insertion_sort2(dp + s, dr + s, len);
+    }
+    __syncthreads();
+    const int nl = wbuf[TB_LONG];
+    for (int l = 0; l < nl; l++) {
+      const int i = cur[l];
+      const int s = cnt[i], len = cnt[i + 1] - s;
+      if (fits) {
+        bitonic_block(sp + s, len);
+        bitonic_block(sr + s, len);
+      } else {
+        sort_segment(dp + s, len, sp, a.cap);
+        sort_segment(dr + s, len, sp, a.cap);
+      }
+    }
+    if (fits) {
+      for (int i = tid; i < n; i += TB_T) {
+        const int p = sp[i];
+        a.perm[s0 + i] = p;
+        a.t_indices[s0 + i] = sr[i];
+        if (a.t_vals) {
+          if (a.vsize == 4) ((int32_t *)a.t_vals)[s0 + i] = __ldg((const int32_t *)a.vals + p);
+          else ((uint16_t *)a.t_vals)[s0 + i] = __ldg((const unsigned short *)a.vals + p);
+        }
+      }
+    } else if (a.t_vals) {
+      for (int i = tid; i < n; i += TB_T) {
+        const int p = a.perm[s0 + i];
+        if (a.vsize == 4) ((int32_t *)a.t_vals)[s0 + i] = __ldg((const int32_t *)a.vals + p);
+        else ((uint16_t *)a.t_vals)[s0 + i] = __ldg((const unsigned short *)a.vals + p);
+      }
+    }
+    __syncthreads();  // the next bucket reuses the shared memory
+  }
+}
+
+static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t *t_indptr, int32_t *t_indices,
+                                  int32_t *perm, void *t_vals, const BucketWs &w, cudaStream_t s) {
+  const int M = A->nrow, K = A->ncol, nnz = A->nnz;
+  const int sms = sm_count();
+  cudaError_t e = cudaMemsetAsync(w.count, 0, (size_t)pl.NB * 4, s);
+  if (e != cudaSuccess) return cuda_fail(e, "transpose clear");
+  const size_t hist_smem = (size_t)pl.NB * 4;
+  const size_t part_smem = (size_t)(2 * pl.NB + TB_E) * 4;
+  const size_t sort_smem = (size_t)(2 * pl.F + 1 + 64 + 2 * pl.cap) * 4;
+  e = cudaFuncSetAttribute(bucket_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(bucket_partition_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem);
+  if (e != cudaSuccess) return cuda_fail(e, "transpose attributes");
+  const long long tiles = ((long long)nnz + TB_E - 1) / TB_E;
+  const int count_blocks = (int)std::min<long long>(((long long)nnz + 4 * TB_T - 1) / (4 * TB_T), 2LL * sms);
+  bucket_count_kernel<<<count_blocks, TB_T, hist_smem, s>>>(A->indices, nnz, K, pl.f, pl.NB, w.count);
+  bucket_scan_kernel<<<1, TB_T, 0, s>>>(w.count, pl.NB, nnz, K, w.start, w.cursor, t_indptr, perm, t_indices);
+  PartArgs pa;
+  pa.indptr = A->indptr; pa.cols = A->indices;
+  pa.M = M; pa.K = K; pa.nnz = nnz; pa.f = pl.f; pa.NB = pl.NB;
+  pa.cursor = w.cursor; pa.pos = w.pos; pa.row = w.row; pa.col = w.col;
+  bucket_partition_kernel<<<(int)std::min<long long>(tiles, 2LL * sms), TB_T, part_smem, s>>>(pa);
+  SortArgs sa;
+  sa.start = w.start; sa.pos = w.pos; sa.row = w.row; sa.col = w.col;
+  sa.K = K; sa.NB = pl.NB; sa.f = pl.f; sa.F = pl.F; sa.cap = pl.cap;
+  sa.t_indptr = t_indptr; sa.perm = perm; sa.t_indices = t_indices;
+  sa.vals = t_vals ? A->values : nullptr;
+  sa.t_vals = t_vals;
+  sa.vsize = dtype_size(A->value_dtype);
+  bucket_sort_kernel<<<std::min(pl.NB, sms), TB_T, sort_smem, s>>>(sa);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
+}
+
 }  // namespace ss
 
 using namespace ss;
@@ -313,29 +781,51 @@ extern "C" {
 
 ss_status ss_csr_transpose_workspace_size(const ss_csr *A, size_t *bytes) {
   if (!A || !bytes || A->nrow < 0 || A->ncol < 0 || A->nnz < 0) return fail(SS_ERR_INVALID_ARG, "bad arguments");
-  *bytes = transpose_ws_bytes(A->ncol, A->nnz, nullptr, nullptr);
+  const BucketPlan pl = bucket_plan(A->ncol, A->nnz);
+  *bytes = pl.ok ? bucket_ws_bytes(pl, A->nnz, nullptr, nullptr) : transpose_ws_bytes(A->ncol, A->nnz, nullptr, nullptr);
   return SS_OK;
 }
 
-ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indices, int32_t *perm, void *ws,
-                           size_t ws_bytes, void *stream) {
+ss_status ss_csr_transpose_values(const ss_csr *A, int32_t *t_indptr, int32_t *t_indices, int32_t *perm,
+                                  void *t_values, void *ws, size_t ws_bytes, void *stream) {
   ss::NvtxRange nvtx_range("ss_csr_transpose");
   if (!A || A->nrow < 0 || A->ncol < 0 || A->nnz < 0) return fail(SS_ERR_INVALID_ARG, "bad CSR descriptor");
   const int M = A->nrow, K = A->ncol, nnz = A->nnz;
   if (!t_indptr || (nnz > 0 && (!t_indices || !perm || !A->indices || !A->indptr)))
     return fail(SS_ERR_INVALID_ARG, "null pointer");
-  const size_t need = transpose_ws_bytes(K, nnz, nullptr, nullptr);
+  if (t_values && nnz > 0 && !A->values) return fail(SS_ERR_INVALID_ARG, "t_values given but A has no values");
+  if (t_values && (A->value_dtype < SS_F32 || A->value_dtype > SS_F16))
+    return fail(SS_ERR_INVALID_ARG, "value_dtype %d unknown", A->value_dtype);
+  const BucketPlan pl = bucket_plan(K, nnz);
+  const size_t need = pl.ok ? bucket_ws_bytes(pl, nnz, nullptr, nullptr) : transpose_ws_bytes(K, nnz, nullptr, nullptr);
   if (ws_bytes < need || !ws || ((uintptr_t)ws % 256))
     return fail(SS_ERR_WORKSPACE, "workspace needs %zu bytes (256-byte aligned), got %zu", need, ws_bytes);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nnz == 0 || K == 0) {  // no entries: t_indptr = zeros; nonzeros with no valid column get -1
+    cudaError_t e = cudaMemsetAsync(t_indptr, 0, (size_t)(K + 1) * 4, s);
+    if (e == cudaSuccess && nnz > 0) e = cudaMemsetAsync(perm, 0xff, (size_t)nnz * 4, s);
+    if (e == cudaSuccess && nnz > 0) e = cudaMemsetAsync(t_indices, 0xff, (size_t)nnz * 4, s);
+    return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose clear");
+  }
+  if (pl.ok) {
+    BucketWs w;
+    bucket_ws_bytes(pl, nnz, &w, ws);
+    return bucket_transpose(A, pl, t_indptr, t_indices, perm, t_values, w, s);
+  }
   TransposeWs w;
   transpose_ws_bytes(K, nnz, &w, ws);
-  cudaStream_t s = (cudaStream_t)stream;
   ss_status st = counting_sort(A->indices, nnz, K, t_indptr, perm, w, s);
-  if (st != SS_OK || nnz == 0 || K == 0) return st;
+  if (st != SS_OK) return st;
   rowid_kernel<<<grid_for((nnz + ROWID_RUN - 1) / ROWID_RUN, 256), 256, 0, s>>>(A->indptr, M, nnz, w.rowid);
   gather_rows_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(perm, w.rowid, nnz, t_indices);
   cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
+  if (e != cudaSuccess) return cuda_fail(e, "transpose launch");
+  return t_values ? ss_gather_values(A->values, A->value_dtype, perm, nnz, t_values, stream) : SS_OK;
+}
+
+ss_status ss_csr_transpose(const ss_csr *A, int32_t *t_indptr, int32_t *t_indices, int32_t *perm, void *ws,
+                           size_t ws_bytes, void *stream) {
+  return ss_csr_transpose_values(A, t_indptr, t_indices, perm, nullptr, ws, ws_bytes, stream);
 }
 
 ss_status ss_coo_to_csr_workspace_size(int nrow, int nnz, size_t *bytes) {

@@ -206,6 +206,25 @@ def compare(rows: Sequence[Row], base: str, action: str) -> dict:
                 faster=sum(1 for x in r if x > 1))
 
 
+def per_strategy(rows: Sequence[Row], defaults: dict) -> dict:
+    """README.md's tables 4 and 5 per strategy and width: over the datasets,
+    the speed-up of the strategy's best tuple over its default tuple
+    (table 4) and cuSPARSE time / the strategy's best time (table 5).
+    defaults[N][strategy] is the default tuple's label."""
+    out: dict = {}
+    widths = sorted({r.N for r in rows})
+    for N in widths:
+        sub = [r for r in rows if r.N == N]
+        for strategy, default in sorted(defaults.get(N, {}).items()):
+            cands = sorted({r.action for r in sub if r.kind == "library" and r.action.startswith(strategy + "(")})
+            if default not in cands:
+                continue
+            t = tuning(sub, default, cands)
+            out[f"{strategy}@N={N}"] = {"datasets": t["datasets"], "tuning_speedup": t["tuning_speedup"],
+                                        "vs_cusparse": t.get("vs_cusparse")}
+    return out
+
+
 def _name(key: tuple[str, int]) -> str:
     return f"{key[0]}@N={key[1]}"
 
@@ -213,14 +232,23 @@ def _name(key: tuple[str, int]) -> str:
 def main(argv=None):
     ap = argparse.ArgumentParser(description="ratio summaries of a sweep table")
     ap.add_argument("table")
-    ap.add_argument("--default", required=True, help="the fixed action the tuning speed-up is measured against")
+    ap.add_argument("--default", help="the fixed action the tuning speed-up is measured against")
     ap.add_argument("--compare", nargs=2, action="append", default=[], metavar=("BASE", "ACTION"))
     ap.add_argument("--epsilon", type=float, default=0.01)
+    ap.add_argument("--per-strategy", metavar="DEFAULTS_JSON",
+                    help="the JSON line `segscan_gb300.sweep` printed: adds the per-strategy tables")
     a = ap.parse_args(argv)
     rows = read_csv(a.table)
-    out = {"tuning": tuning(rows, a.default), "static": static_ranking(rows, epsilon=a.epsilon)}
-    out["static"].pop("all")
+    out = {}
+    if a.default:
+        out = {"tuning": tuning(rows, a.default), "static": static_ranking(rows, epsilon=a.epsilon)}
+        out["static"].pop("all")
     out["compare"] = [compare(rows, b, x) for b, x in a.compare]
+    if a.per_strategy:
+        with open(a.per_strategy) as f:
+            line = [ln for ln in f if ln.strip().startswith("{")][-1]
+        defaults = {int(n): d for n, d in json.loads(line)["defaults"].items()}
+        out["per_strategy"] = per_strategy(rows, defaults)
     print(json.dumps(out, indent=1))
 
 

@@ -55,6 +55,22 @@ def test_compare_base_over_action():
         ratios.compare(table(), "dg", "missing")
 
 
+def test_per_strategy_tables():
+    rows = [
+        Row("a", 4, "cusparse", "cusparse", 40.0), Row("b", 4, "cusparse", "cusparse", 12.0),
+        Row("a", 4, "ebsr(1,2)", "library", 20.0), Row("a", 4, "ebsr(3,4)", "library", 10.0),
+        Row("b", 4, "ebsr(1,2)", "library", 15.0), Row("b", 4, "ebsr(3,4)", "library", 30.0),
+        Row("a", 4, "rbsr(5)", "library", 8.0), Row("b", 4, "rbsr(5)", "library", 24.0),
+    ]
+    out = ratios.per_strategy(rows, {4: {"ebsr": "ebsr(1,2)", "rbsr": "rbsr(5)", "ebpr": "ebpr(9)"}})
+    assert set(out) == {"ebsr@N=4", "rbsr@N=4"}  # no ebpr rows: left out
+    e = out["ebsr@N=4"]  # best a: 10 (2x over the default), b: the default 15 (1x)
+    assert math.isclose(e["tuning_speedup"]["gmean"], math.sqrt(2.0)) and e["tuning_speedup"]["max"] == 2.0
+    assert math.isclose(e["vs_cusparse"]["gmean"], math.sqrt(4.0 * 0.8))  # 40/10, 12/15
+    r = out["rbsr@N=4"]  # one tuple: no tuning gain; cuSPARSE 40/8 and 12/24
+    assert r["tuning_speedup"]["max"] == 1.0 and math.isclose(r["vs_cusparse"]["gmean"], math.sqrt(5.0 * 0.5))
+
+
 def test_csv_round_trip(tmp_path):
     p = tmp_path / "t.csv"
     ratios.write_csv(p, table())
