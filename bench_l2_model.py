@@ -1,0 +1,81 @@
+"""L2 ceiling model for the SpMM row gathers of the power-law workload.
+
+Replays the column stream of A (the order the walk reads B rows: CSR order;
+columns are uniform, so the interleaving of concurrent chunks does not
+change the reuse statistics) through an ideal LRU cache of B rows, for the
+whole L2 and for the share one die's SMs can use, and turns the miss counts
+into DRAM bytes and a lower bound on the launch time at a given DRAM rate:
+
+    python bench_l2_model.py --N 64 --l2-mb 126 63 --dram-gbs 5100
+
+DRAM bytes per launch = misses * row bytes + A's streams (indptr, indices,
+values) + C's writes.  The algorithmic bytes count each distinct B row once,
+so the ratio of the two is the traffic the cache capacity forces, and
+algorithmic bytes / (DRAM bytes / rate) is the highest algorithmic fraction
+a kernel can reach at that rate.  CPU only; takes about ten seconds per
+capacity.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+from collections import OrderedDict
+
+import numpy as np
+
+from segscan_gb300 import synth
+
+
+def lru_misses(stream: np.ndarray, lines: int) -> int:
+    """Misses of a fully associative LRU cache of `lines` entries."""
+    cache: OrderedDict = OrderedDict()
+    misses = 0
+    for x in stream.tolist():
+        if x in cache:
+            cache.move_to_end(x)
+        else:
+            misses += 1
+            cache[x] = None
+            if len(cache) > lines:
+                cache.popitem(last=False)
+    return misses
+
+
+def model(A: synth.Csr, N: int, l2_mb: list[float], dram_gbs: float, value_bytes: int = 4) -> dict:
+    row = N * 4
+    distinct = int(np.unique(A.indices).size)
+    streams = A.nnz * (4 + value_bytes) + (A.nrow + 1) * 4
+    c_bytes = A.nrow * N * 4
+    alg = streams + distinct * row + c_bytes
+    out = {"nnz": A.nnz, "distinct_columns": distinct, "row_bytes": row, "algorithmic_mb": round(alg / 1e6, 1),
+           "compulsory_hit_ceiling": round(1 - distinct / A.nnz, 4), "capacities": []}
+    for mb in l2_mb:
+        lines = int(mb * 1e6 / row)
+        miss = lru_misses(A.indices, lines)
+        dram = streams + miss * row + c_bytes
+        t_us = dram / (dram_gbs * 1e3)
+        out["capacities"].append({
+            "l2_mb": mb, "lines": lines, "hit_rate": round(1 - miss / A.nnz, 4),
+            "dram_mb": round(dram / 1e6, 1), "traffic_over_alg": round(dram / alg, 3),
+            "time_us_at_rate": round(t_us, 1), "alg_gbs_ceiling": round(alg / t_us / 1e3, 1)})
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--N", type=int, default=64)
+    ap.add_argument("--l2-mb", type=float, nargs="+", default=[126.0, 63.0])
+    ap.add_argument("--dram-gbs", type=float, default=5100.0,
+                    help="DRAM rate of random row reads mixed with C writes")
+    ap.add_argument("--peak-gbs", type=float, default=None, help="adds alg_gbs_ceiling / peak")
+    a = ap.parse_args(argv)
+    A = synth.powerlaw(1_000_000, 1_000_000, 2.1, 1, 20000, seed=1)
+    out = model(A, a.N, a.l2_mb, a.dram_gbs)
+    if a.peak_gbs:
+        for c in out["capacities"]:
+            c["frac_ceiling"] = round(c["alg_gbs_ceiling"] / a.peak_gbs, 3)
+    print(json.dumps(out, indent=1))
+
+
+if __name__ == "__main__":
+    main()

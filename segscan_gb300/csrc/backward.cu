@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
           #pragma unroll
           for (int i = 0; i < V; i++) {
             part[u] = fmaf(g[u][j][i], b[j][i], part[u]);
-            if (kahan) kahan_add(acc[j][i], comp[j][i], av[u] * g[u][j][i]);
+            if (kahan) kahan_fma(acc[j][i], comp[j][i], av[u], g[u][j][i]);
             else acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
           }
       }

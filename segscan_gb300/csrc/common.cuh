@@ -288,10 +288,17 @@ __device__ __forceinline__ float butterfly_sum(float (&v)[U], int lane, int lane
 
 // Compensated (Kahan) accumulation step: acc += x with running error c.
 __device__ __forceinline__ void kahan_add(float &acc, float &c, float x) {
-  float y = x - c;
-  float t = acc + y;
-  c = (t - acc) - y;
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(acc, y);
+  c = __fsub_rn(__fsub_rn(t, acc), y);
   acc = t;
+}
+
+// acc += v * b with compensation.  The product is rounded on its own
+// (__fmul_rn is never contracted into an FMA with the step that follows), so
+// every kernel that sums the same terms in the same order gets the same bits.
+__device__ __forceinline__ void kahan_fma(float &acc, float &c, float v, float b) {
+  kahan_add(acc, c, __fmul_rn(v, b));
 }
 
 // Lane mask of the aligned sub-warp of `width` lanes containing this lane.

@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(512) eb_narrow_kernel(EbArgs a) {
         for (int j = 0; j < NV; j++)
           #pragma unroll
           for (int i = 0; i < V; i++) {
-            if (kahan) kahan_add(acc[j][i], comp[j][i], v[u] * b[u][j][i]);
+            if (kahan) kahan_fma(acc[j][i], comp[j][i], v[u], b[u][j][i]);
             else acc[j][i] = fmaf(v[u], b[u][j][i], acc[j][i]);
           }
       }

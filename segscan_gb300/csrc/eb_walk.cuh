@@ -146,7 +146,7 @@ __device__ __forceinline__ void add_row(float (&acc)[NV][V], float (&comp)[NV][V
   for (int j = 0; j < NV; j++)
     #pragma unroll
     for (int i = 0; i < V; i++) {
-      if (KAHAN) kahan_add(acc[j][i], comp[j][i], v * b[j][i]);
+      if (KAHAN) kahan_fma(acc[j][i], comp[j][i], v, b[j][i]);
       else acc[j][i] = fmaf(v, b[j][i], acc[j][i]);
     }
 }
@@ -504,7 +504,11 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
   __syncwarp(mask);
   for (int i = lane; i < L.W; i += G) st.win[i] = __ldg(a.indptr + min(base + i, a.M));
   __syncwarp(mask);
-  if (chunk_has_long_row(a, st, L, cs, ce, lane, G, mask))
+  // groups sharing a warp take the same walk (either gives the same bits for
+  // a chunk without long rows), so the warp does not run both one after the
+  // other
+  const bool kah = __any_sync(__activemask(), chunk_has_long_row(a, st, L, cs, ce, lane, G, mask));
+  if (kah)
     return sr_spmm_walk<T, TC, V, NV, true>(a, chunk, cs, ce, nst, lb, base, lane, mask, st, L, col0, act, keep,
                                             strm);
   return sr_spmm_walk<T, TC, V, NV, false>(a, chunk, cs, ce, nst, lb, base, lane, mask, st, L, col0, act, keep,

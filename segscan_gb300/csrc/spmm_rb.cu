@@ -137,7 +137,7 @@ __device__ __forceinline__ void rbsr_row(const RbArgs &a, int s, int e, int lane
         for (int j = 0; j < NV; j++)
           #pragma unroll
           for (int i = 0; i < V; i++) {
-            if (KAHAN) kahan_add(acc.v[j][i], comp.v[j][i], v[u] * b[u][j][i]);
+            if (KAHAN) kahan_fma(acc.v[j][i], comp.v[j][i], v[u], b[u][j][i]);
             else acc.v[j][i] = fmaf(v[u], b[u][j][i], acc.v[j][i]);
           }
     }
@@ -237,7 +237,7 @@ __device__ __forceinline__ void rbpr_slot(const RbArgs &a, int s, int e, int slo
       for (int j = 0; j < NV; j++)
         #pragma unroll
         for (int i = 0; i < V; i++) {
-          if (KAHAN) kahan_add(acc.v[j][i], comp.v[j][i], v[u] * b[u][j][i]);
+          if (KAHAN) kahan_fma(acc.v[j][i], comp.v[j][i], v[u], b[u][j][i]);
           else acc.v[j][i] = fmaf(v[u], b[u][j][i], acc.v[j][i]);
         }
   }
