@@ -19,9 +19,9 @@
 //  * four B rows are gathered ahead of the multiply-adds, with registers
 //    capped at 64 so that 32+ warps per SM keep enough gathers in flight;
 //  * rows longer than kahan_threshold accumulate with compensated
-//    summation, every nonzero of them: a chunk that touches such a row (read
-//    off the staged indptr window) takes the walk whose tile labelling marks
-//    their nonzeros; other chunks take a walk without compensation terms;
+//    summation, every nonzero of them: the tile labelling marks their
+//    nonzeros (one bit each), and the multiply-add of a marked nonzero is a
+//    compensated step;
 //  * a row is flushed when the walk passes its end (eb_common.cuh: owner
 //    store, head/tail slots for the two rows that straddle the chunk,
 //    zeros for empty rows).
@@ -190,34 +190,13 @@ __device__ __forceinline__ void store_out(const EbArgs &a, int row, float (&acc)
   }
 }
 
-// True when a row with more than a.kahan nonzeros overlaps [cs, ce).  The
-// window holds indptr from win_base on, win_base being the row that holds
-// cs or an earlier one; every row it covers is checked.  When the chunk
-// runs past the window, the rows wholly inside the chunk are no longer than
-// the chunk, so only the row holding ce - 1 is left to look up (a chunk
-// longer than the threshold is then taken as holding a long row).
-__device__ __forceinline__ bool chunk_has_long_row(const EbArgs &a, const Stage &st, const SrLayout &L, int cs,
-                                                   int ce, int lane, int G, unsigned mask) {
-  bool found = false;
-  for (int i = lane; i < L.W - 1; i += G) {
-    const int s = st.win[i], e = st.win[i + 1];
-    found |= s < ce && e > cs && e - s > a.kahan;
-  }
-  found = __any_sync(mask, found);
-  if (found || st.win[L.W - 1] >= ce) return found;  // entries past row M hold nnz
-  if (ce - cs > a.kahan) return true;
-  const int r = group_lower_bound(a.indptr, a.M, ce, lane, G, mask);  // row r - 1 holds ce - 1
-  return __ldg(a.indptr + r) - __ldg(a.indptr + r - 1) > a.kahan;
-}
-
 // Walks nonzeros [cs, ce) as work item `chunk` (its head / tail slots); the
 // first two tiles are in flight, lb is the first row starting at or after
-// cs and the window holds indptr from win_base on.  KAH: some row of the
-// chunk is longer than a.kahan; the tile labelling then marks the nonzeros
-// of such rows, which are summed with compensation.  Without KAH the walk
-// carries no compensation terms at all, which keeps it within its register
-// budget.  Returns false when a bounded wait expired (the caller then stops).
-template <typename T, typename TC, int V, int NV, bool KAH>
+// cs and the window holds indptr from win_base on.  The tile labelling marks
+// the nonzeros of rows longer than a.kahan (kmask), which are summed with
+// compensation.  Returns false when a bounded wait expired (the caller then
+// stops).
+template <typename T, typename TC, int V, int NV>
 __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs, int ce, int nst, int lb,
                                              int win_base, int lane, unsigned mask, Stage &st, const SrLayout &L,
                                              int col0, const bool (&act)[NV], uint64_t keep, uint64_t strm) {
@@ -225,9 +204,11 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
   const int G = a.team_lanes;
   const bool ones = a.vals == nullptr;
   // B rows gathered ahead: four, or two when a lane holds 8+ elements of a
-  // row (the gathered values then need as many registers)
+  // row (the gathered values then need as many registers), except that the
+  // full-tile loop keeps four 16-bit rows of eight elements packed
   constexpr int SR_FU = V * NV >= 8 ? 2 : 4;
   constexpr int SR_UP = V * NV >= 8 ? 2 : SR_U;
+  constexpr bool PACKED = sizeof(T) == 2 && V == 8 && NV == 1;
   ChunkInfo ci;
   ci.cs = cs;
   ci.ce = ce;
@@ -299,10 +280,10 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
     const bool fast = st.win[L.W - 1] > last || win_base + L.W - 1 >= a.M;
 
     if (fast) {
-      // ---- label the tile's nonzeros with row | end-of-row bit (and, with
-      // KAH, mark those of long rows: kmask bit e); empty rows starting where
-      // a row's first nonzero sits are zeroed by the whole group (each lane
-      // owns one column slice)
+      // ---- label the tile's nonzeros with row | end-of-row bit, and mark
+      // those of long rows (kmask bit e); empty rows starting where a row's
+      // first nonzero sits are zeroed by the whole group (each lane owns one
+      // column slice)
       const int c0 = cur - win_base;
       const int rounds = (n + G - 1) / G;
       bool bad = false;  // a column outside [0, K) in this tile
@@ -321,7 +302,7 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
           }
           const int rr = lo - 1;  // window slot of p's row
           const bool end = st.win[rr + 1] == p + 1;
-          if (KAH) kah = st.win[rr + 1] - st.win[rr] > a.kahan;
+          kah = st.win[rr + 1] - st.win[rr] > a.kahan;
           sinfo[e] = (win_base + rr) | (end ? (int)0x80000000 : 0);
           if (st.win[rr] == p && p != ci.cs) {  // p opens row rr: empties before it start at p too
             int q = rr - 1;
@@ -330,7 +311,7 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
             zhi = win_base + rr - 1;
           }
         }
-        if (KAH) kmask |= (uint64_t)group_ballot(mask, kah, G) << (k * G);
+        kmask |= (uint64_t)group_ballot(mask, kah, G) << (k * G);
         unsigned todo = __ballot_sync(mask, zlo <= zhi);
         while (todo) {
           const int src = __ffs(todo) - 1;
@@ -345,8 +326,7 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
       // columns, labels and values per shared-memory read, no bounds checks
       const bool full = n == L.S && !__any_sync(mask, bad);
       auto consume = [&](int info, float v, const float (&b)[NV][V], bool kah) {
-        if (KAH) add_row<V, NV>(acc, comp, v, b, kah);
-        else add_row<V, NV, false>(acc, comp, v, b);
+        add_row<V, NV>(acc, comp, v, b, kah);
         cur = info & 0x7fffffff;
         open = true;
         if (info < 0) {
@@ -373,23 +353,41 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
             unpack2(x.x, v4[0], v4[1], (T *)nullptr);
             unpack2(x.y, v4[2], v4[3], (T *)nullptr);
           }
-          const unsigned k4 = KAH ? (unsigned)(kmask >> q) & 0xfu : 0u;  // compensated among these four
-          #pragma unroll
-          for (int h = 0; h < 4; h += SR_FU) {
-            float bv[SR_FU][NV][V];
+          const unsigned k4 = (unsigned)(kmask >> q) & 0xfu;  // compensated among these four
+          if constexpr (PACKED) {
+            // 16-bit rows of one 16-byte vector per lane: the four rows stay
+            // packed (four registers each) until their multiply-adds
+            uint4 raw[4];
             #pragma unroll
-            for (int u = 0; u < SR_FU; u++)
+            for (int u = 0; u < 4; u++)
+              raw[u] = act[0] ? ld_u128(B + (int64_t)cs4[u] * a.N + col0, keep) : make_uint4(0, 0, 0, 0);
+            #pragma unroll
+            for (int u = 0; u < 4; u++) {
+              float bv[1][V];
+              unpack2(raw[u].x, bv[0][0], bv[0][1], (T *)nullptr);
+              unpack2(raw[u].y, bv[0][2], bv[0][3], (T *)nullptr);
+              unpack2(raw[u].z, bv[0][4], bv[0][5], (T *)nullptr);
+              unpack2(raw[u].w, bv[0][6], bv[0][7], (T *)nullptr);
+              consume(is4[u], v4[u], reinterpret_cast<const float(&)[NV][V]>(bv), (k4 >> u) & 1u);
+            }
+          } else {
+            #pragma unroll
+            for (int h = 0; h < 4; h += SR_FU) {
+              float bv[SR_FU][NV][V];
               #pragma unroll
-              for (int j = 0; j < NV; j++) {
-                if (act[j]) {
-                  load_vec<T, V>(B + (int64_t)cs4[h + u] * a.N + col0 + j * V, bv[u][j], keep);
-                } else {
-                  #pragma unroll
-                  for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+              for (int u = 0; u < SR_FU; u++)
+                #pragma unroll
+                for (int j = 0; j < NV; j++) {
+                  if (act[j]) {
+                    load_vec<T, V>(B + (int64_t)cs4[h + u] * a.N + col0 + j * V, bv[u][j], keep);
+                  } else {
+                    #pragma unroll
+                    for (int i = 0; i < V; i++) bv[u][j][i] = 0.f;
+                  }
                 }
-              }
-            #pragma unroll
-            for (int u = 0; u < SR_FU; u++) consume(is4[h + u], v4[h + u], bv[u], (k4 >> (h + u)) & 1u);
+              #pragma unroll
+              for (int u = 0; u < SR_FU; u++) consume(is4[h + u], v4[h + u], bv[u], (k4 >> (h + u)) & 1u);
+            }
           }
         }
       } else for (int q = 0; q < n; q += SR_UP) {  // ---- partial tile: gather, multiply, store at row ends
@@ -426,7 +424,7 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
           if (next_start <= sb && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
         }
       }
-      bool kah = KAH && next_start - wget(cur) > a.kahan;  // row cur is compensated
+      bool kah = next_start - wget(cur) > a.kahan;  // row cur is compensated
       for (int q = 0; q < n; q++) {
         const int p = sb + q;
         const int c = scol[q];
@@ -449,11 +447,10 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
             if (ns <= p && !a.accumulate) zero_rows<TC, V, NV>(a, cur, cur, col0, act, strm);
           } while (ns <= p && cur < a.M - 1);
           next_start = ns;
-          kah = KAH && next_start - wget(cur) > a.kahan;
+          kah = next_start - wget(cur) > a.kahan;
         }
         const float v = ones ? 1.f : Elem<T>::to_f(sval[q]);
-        if (KAH) add_row<V, NV>(acc, comp, v, bq, kah);
-        else add_row<V, NV, false>(acc, comp, v, bq);
+        add_row<V, NV>(acc, comp, v, bq, kah);
         open = true;
       }
       // close a row that ends exactly at the tile end; the next tile zeroes
@@ -486,9 +483,9 @@ __device__ __forceinline__ bool sr_spmm_walk(const EbArgs &a, int chunk, int cs,
 // Walks nonzeros [cs, ce) as work item `chunk`.  Element-balanced items are
 // chunk * a.chunk onwards; a row-balanced item (batched) starts and ends on
 // row boundaries, so no row straddles it.  The first two tiles are issued,
-// the first row searched and the indptr window filled from the row holding
-// cs; the walk is then the compensated one only when the chunk touches a row
-// longer than a.kahan.  Returns false when a bounded wait expired.
+// the first row searched and the indptr window filled from the row before
+// it (which holds cs when the chunk starts inside a row).  Returns false
+// when a bounded wait expired.
 template <typename T, typename TC, int V, int NV>
 __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs, int ce, int lane, unsigned mask,
                                               Stage &st, const SrLayout &L, int col0, const bool (&act)[NV],
@@ -497,22 +494,12 @@ __device__ __forceinline__ bool sr_spmm_chunk(const EbArgs &a, int chunk, int cs
   const int nst = (ce - cs + L.S - 1) / L.S;
   stage_issue<T, false>(a, st, L, 0, cs, min(L.S, ce - cs), lane, G, mask, strm);
   if (nst > 1) stage_issue<T, false>(a, st, L, 1, cs + L.S, min(L.S, ce - cs - L.S), lane, G, mask, strm);
-  // lb = first row starting at or after cs; the window starts at the row
-  // before it, which holds cs when the chunk starts inside a row
   const int lb = group_lower_bound(a.indptr, a.M, cs, lane, G, mask);
   const int base = lb > 0 ? lb - 1 : 0;
   __syncwarp(mask);
   for (int i = lane; i < L.W; i += G) st.win[i] = __ldg(a.indptr + min(base + i, a.M));
   __syncwarp(mask);
-  // groups sharing a warp take the same walk (either gives the same bits for
-  // a chunk without long rows), so the warp does not run both one after the
-  // other
-  const bool kah = __any_sync(__activemask(), chunk_has_long_row(a, st, L, cs, ce, lane, G, mask));
-  if (kah)
-    return sr_spmm_walk<T, TC, V, NV, true>(a, chunk, cs, ce, nst, lb, base, lane, mask, st, L, col0, act, keep,
-                                            strm);
-  return sr_spmm_walk<T, TC, V, NV, false>(a, chunk, cs, ce, nst, lb, base, lane, mask, st, L, col0, act, keep,
-                                           strm);
+  return sr_spmm_walk<T, TC, V, NV>(a, chunk, cs, ce, nst, lb, base, lane, mask, st, L, col0, act, keep, strm);
 }
 
 // ---------------------------------------------------------------------
