@@ -332,13 +332,15 @@ static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out
 // ---------------------------------------------------------------------
 // Two-level bucket transpose (ss_csr_transpose)
 // ---------------------------------------------------------------------
-constexpr int TB_T = 1024;           // threads per block (partition and sort)
-constexpr int TB_PER = 8;            // nonzeros per thread in a partition tile
-constexpr int TB_E = TB_T * TB_PER;  // nonzeros per partition tile
+constexpr int TB_T = 1024;            // threads per block (count, scan)
+constexpr int TB_PT = 512;            // threads per block (partition; two blocks per SM)
+constexpr int TB_PER = 8;             // nonzeros per thread in a partition tile
+constexpr int TB_E = TB_PT * TB_PER;  // nonzeros per partition tile
+constexpr int TB_ST = 512;            // threads per block (bucket sort; two blocks per SM)
 constexpr int TB_F_LOG2_MAX = 13;  // at most 8192 columns per bucket
 constexpr int TB_NB_MAX = 8192;    // buckets
 #ifndef SS_TB_SORT_SMEM_KB
-#define SS_TB_SORT_SMEM_KB 220
+#define SS_TB_SORT_SMEM_KB 110
 #endif
 constexpr int TB_SORT_SMEM = SS_TB_SORT_SMEM_KB * 1024;
 constexpr int TB_LONG = 40;  // slot of the long-column count in the sort block's scratch
@@ -524,7 +526,7 @@ struct PartArgs {
 
 // One tile of TB_E nonzeros per round: rows, then (position, row, column)
 // records into the tile's reserved range of each bucket.
-__global__ void __launch_bounds__(TB_T) bucket_partition_kernel(PartArgs a) {
+__global__ void __launch_bounds__(TB_PT, 2) bucket_partition_kernel(PartArgs a) {
   extern __shared__ int32_t sm[];
   int32_t *hist = sm;             // [NB]
   int32_t *base = hist + a.NB;    // [NB]
@@ -539,11 +541,11 @@ __global__ void __launch_bounds__(TB_T) bucket_partition_kernel(PartArgs a) {
       const int r = warp_row_of(a.indptr, a.M, tid < 32 ? b0 : b0 + n - 1, tid & 31);
       if ((tid & 31) == 0) r01[tid >> 5] = r;
     }
-    for (int i = tid; i < a.NB; i += TB_T) hist[i] = 0;
+    for (int i = tid; i < a.NB; i += TB_PT) hist[i] = 0;
     int c[TB_PER], rr[TB_PER];
     #pragma unroll
     for (int k = 0; k < TB_PER; k++) {
-      const int e = tid + k * TB_T;
+      const int e = tid + k * TB_PT;
       c[k] = e < n ? __ldg(a.cols + b0 + e) : -1;
     }
     __syncthreads();
@@ -551,9 +553,9 @@ __global__ void __launch_bounds__(TB_T) bucket_partition_kernel(PartArgs a) {
     if ((long long)(r1 - r0) <= 4LL * TB_E) {
       // mark each row's first nonzero (the last of the rows that start
       // there: rows before it are empty), then a running maximum
-      for (int e = tid; e < TB_E; e += TB_T) rows[e] = e == 0 ? r0 : -1;
+      for (int e = tid; e < TB_E; e += TB_PT) rows[e] = e == 0 ? r0 : -1;
       __syncthreads();
-      for (int r = r0 + 1 + tid; r <= r1; r += TB_T) {
+      for (int r = r0 + 1 + tid; r <= r1; r += TB_PT) {
         const int e = __ldg(a.indptr + r) - b0;
         if ((unsigned)e < (unsigned)TB_E) atomicMax(rows + e, r);
       }
@@ -561,14 +563,14 @@ __global__ void __launch_bounds__(TB_T) bucket_partition_kernel(PartArgs a) {
       block_scan<true>(rows, n, wbuf);
       #pragma unroll
       for (int k = 0; k < TB_PER; k++) {
-        const int e = tid + k * TB_T;
+        const int e = tid + k * TB_PT;
         rr[k] = e < n ? rows[e] : -1;
       }
     } else {
       // long runs of empty rows: a binary search in [r0, r1] per nonzero
       #pragma unroll
       for (int k = 0; k < TB_PER; k++) {
-        const int e = tid + k * TB_T;
+        const int e = tid + k * TB_PT;
         int lo = r0, hi = r1;
         while (lo < hi) {
           const int mid = lo + ((hi - lo + 1) >> 1);
@@ -581,7 +583,7 @@ __global__ void __launch_bounds__(TB_T) bucket_partition_kernel(PartArgs a) {
     for (int k = 0; k < TB_PER; k++)
       if ((unsigned)c[k] < (unsigned)a.K) atomicAdd(hist + (c[k] >> a.f), 1);
     __syncthreads();
-    for (int i = tid; i < a.NB; i += TB_T) {
+    for (int i = tid; i < a.NB; i += TB_PT) {
       const int h = hist[i];
       base[i] = h ? atomicAdd(a.cursor + i, h) : 0;
       hist[i] = 0;
@@ -592,7 +594,7 @@ __global__ void __launch_bounds__(TB_T) bucket_partition_kernel(PartArgs a) {
       if ((unsigned)c[k] < (unsigned)a.K) {
         const int bk = c[k] >> a.f;
         const int q = base[bk] + atomicAdd(hist + bk, 1);
-        a.pos[q] = b0 + tid + k * TB_T;
+        a.pos[q] = b0 + tid + k * TB_PT;
         a.row[q] = rr[k];
         a.col[q] = c[k];
       }
@@ -639,7 +641,7 @@ struct SortArgs {
   int vsize;         // 4 or 2 bytes
 };
 
-__global__ void __launch_bounds__(TB_T, 1) bucket_sort_kernel(SortArgs a) {
+__global__ void __launch_bounds__(TB_ST, 2) bucket_sort_kernel(SortArgs a) {
   extern __shared__ int32_t sm[];
   int32_t *cnt = sm;                 // [F + 1]: counts, then column starts
   int32_t *cur = cnt + a.F + 1;      // [F]: placement cursors, then the long columns
@@ -651,14 +653,14 @@ __global__ void __launch_bounds__(TB_T, 1) bucket_sort_kernel(SortArgs a) {
     const int c0 = b << a.f;
     const int nf = min(a.F, a.K - c0);
     const int s0 = __ldg(a.start + b), n = __ldg(a.start + b + 1) - s0;
-    for (int i = tid; i < nf; i += TB_T) cnt[i] = 0;
+    for (int i = tid; i < nf; i += TB_ST) cnt[i] = 0;
     if (tid == 0) wbuf[TB_LONG] = 0;
     __syncthreads();
-    for (int i0 = 0; i0 < n; i0 += 4 * TB_T) {
+    for (int i0 = 0; i0 < n; i0 += 4 * TB_ST) {
       int c[4];
       #pragma unroll
       for (int u = 0; u < 4; u++) {
-        const int i = i0 + tid + u * TB_T;
+        const int i = i0 + tid + u * TB_ST;
         c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
       }
       #pragma unroll
@@ -667,7 +669,7 @@ __global__ void __launch_bounds__(TB_T, 1) bucket_sort_kernel(SortArgs a) {
     }
     __syncthreads();
     const int total = block_scan<false>(cnt, nf, wbuf);
-    for (int i = tid; i < nf; i += TB_T) {
+    for (int i = tid; i < nf; i += TB_ST) {
       a.t_indptr[c0 + i] = s0 + cnt[i];
       cur[i] = cnt[i];
     }
@@ -678,17 +680,17 @@ __global__ void __launch_bounds__(TB_T, 1) bucket_sort_kernel(SortArgs a) {
     const bool fits = n <= a.cap;
     int32_t *dp = fits ? sp : a.perm + s0;
     int32_t *dr = fits ? sr : a.t_indices + s0;
-    for (int i0 = 0; i0 < n; i0 += 2 * TB_T) {
-      int c[2], p[2], r[2];
+    for (int i0 = 0; i0 < n; i0 += 4 * TB_ST) {
+      int c[4], p[4], r[4];
       #pragma unroll
-      for (int u = 0; u < 2; u++) {
-        const int i = i0 + tid + u * TB_T;
+      for (int u = 0; u < 4; u++) {
+        const int i = i0 + tid + u * TB_ST;
         c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
         p[u] = i < n ? __ldg(a.pos + s0 + i) : 0;
         r[u] = i < n ? __ldg(a.row + s0 + i) : 0;
       }
       #pragma unroll
-      for (int u = 0; u < 2; u++) {
+      for (int u = 0; u < 4; u++) {
         if ((unsigned)c[u] < (unsigned)nf) {
           const int q = atomicAdd(cur + c[u], 1);
           dp[q] = p[u];
@@ -698,7 +700,7 @@ __global__ void __launch_bounds__(TB_T, 1) bucket_sort_kernel(SortArgs a) {
     }
     __syncthreads();
     // each column by position: short ones by a thread, long ones by the block
-    for (int i = tid; i < nf; i += TB_T) {
+    for (int i = tid; i < nf; i += TB_ST) {
       const int s = cnt[i], len = cnt[i + 1] - s;
       if (len > 32) cur[atomicAdd(wbuf + TB_LONG, 1)] = i;
       else if (len > 1) insertion_sort2(dp + s, dr + s, len);
@@ -717,20 +719,28 @@ __global__ void __launch_bounds__(TB_T, 1) bucket_sort_kernel(SortArgs a) {
       }
     }
     if (fits) {
-      for (int i = tid; i < n; i += TB_T) {
-        const int p = sp[i];
-        a.perm[s0 + i] = p;
+      for (int i = tid; i < n; i += TB_ST) {
+        a.perm[s0 + i] = sp[i];
         a.t_indices[s0 + i] = sr[i];
-        if (a.t_vals) {
-          if (a.vsize == 4) ((int32_t *)a.t_vals)[s0 + i] = __ldg((const int32_t *)a.vals + p);
-          else ((uint16_t *)a.t_vals)[s0 + i] = __ldg((const unsigned short *)a.vals + p);
-        }
       }
-    } else if (a.t_vals) {
-      for (int i = tid; i < n; i += TB_T) {
-        const int p = a.perm[s0 + i];
-        if (a.vsize == 4) ((int32_t *)a.t_vals)[s0 + i] = __ldg((const int32_t *)a.vals + p);
-        else ((uint16_t *)a.t_vals)[s0 + i] = __ldg((const unsigned short *)a.vals + p);
+    }
+    if (a.t_vals) {  // the values, eight gathers in flight per thread
+      const int32_t *src = fits ? sp : a.perm + s0;
+      for (int i0 = 0; i0 < n; i0 += 8 * TB_ST) {
+        uint32_t v[8];
+        #pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int i = i0 + tid + u * TB_ST;
+          const int p = i < n ? src[i] : 0;
+          v[u] = a.vsize == 4 ? __ldg((const uint32_t *)a.vals + p) : __ldg((const unsigned short *)a.vals + p);
+        }
+        #pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int i = i0 + tid + u * TB_ST;
+          if (i >= n) break;
+          if (a.vsize == 4) ((uint32_t *)a.t_vals)[s0 + i] = v[u];
+          else ((uint16_t *)a.t_vals)[s0 + i] = (uint16_t)v[u];
+        }
       }
     }
     __syncthreads();  // the next bucket reuses the shared memory
@@ -760,7 +770,7 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   pa.indptr = A->indptr; pa.cols = A->indices;
   pa.M = M; pa.K = K; pa.nnz = nnz; pa.f = pl.f; pa.NB = pl.NB;
   pa.cursor = w.cursor; pa.pos = w.pos; pa.row = w.row; pa.col = w.col;
-  bucket_partition_kernel<<<(int)std::min<long long>(tiles, 2LL * sms), TB_T, part_smem, s>>>(pa);
+  bucket_partition_kernel<<<(int)std::min<long long>(tiles, 2LL * sms), TB_PT, part_smem, s>>>(pa);
   SortArgs sa;
   sa.start = w.start; sa.pos = w.pos; sa.row = w.row; sa.col = w.col;
   sa.K = K; sa.NB = pl.NB; sa.f = pl.f; sa.F = pl.F; sa.cap = pl.cap;
@@ -768,7 +778,7 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   sa.vals = t_vals ? A->values : nullptr;
   sa.t_vals = t_vals;
   sa.vsize = dtype_size(A->value_dtype);
-  bucket_sort_kernel<<<std::min(pl.NB, sms), TB_T, sort_smem, s>>>(sa);
+  bucket_sort_kernel<<<std::min(pl.NB, 2 * sms), TB_ST, sort_smem, s>>>(sa);
   e = cudaGetLastError();
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
 }

@@ -6,19 +6,30 @@
 
 namespace ss {
 
-int sm_count() {
-  static std::atomic<int> cache[64];  // 0 = not looked up yet
+// A device attribute of the current device, cached per device; `fallback`
+// when it cannot be read.
+static int device_attr(cudaDeviceAttr attr, std::atomic<int> (&cache)[64], int fallback) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fallback;
   if (dev < 0 || dev >= 64) {
     int n = 0;
-    return cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 1;
+    return cudaDeviceGetAttribute(&n, attr, dev) == cudaSuccess && n > 0 ? n : fallback;
   }
   int n = cache[dev].load(std::memory_order_relaxed);
   if (n > 0) return n;
-  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 1;
+  if (cudaDeviceGetAttribute(&n, attr, dev) != cudaSuccess || n <= 0) return fallback;
   cache[dev].store(n, std::memory_order_relaxed);  // every thread stores the same value
   return n;
+}
+
+int sm_count() {
+  static std::atomic<int> cache[64];  // 0 = not looked up yet
+  return device_attr(cudaDevAttrMultiProcessorCount, cache, 1);
+}
+
+int max_smem_per_block() {
+  static std::atomic<int> cache[64];
+  return device_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, cache, 48 * 1024);
 }
 
 // rows[i] = binary_search_segment_number(indptr, M, nnz, e) for e = elems[i]
