@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
           #pragma unroll
           for (int i = 0; i < V; i++) {
             part[u] = fmaf(g[u][j][i], b[j][i], part[u]);
-            if (kahan) kahan_fma(acc[j][i], comp[j][i], av[u], g[u][j][i]);
-            else acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
+            if (!kahan) acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
+            else if (q0 + u < e) kahan_fma(acc[j][i], comp[j][i], av[u], g[u][j][i]);  // not past the row
           }
       }
       // the four dot products: reduced across the lanes, stored at A's positions

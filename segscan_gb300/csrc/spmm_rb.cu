@@ -131,14 +131,19 @@ __device__ __forceinline__ void rbsr_row(const RbArgs &a, int s, int e, int lane
         }
         if (!live) v[u] = 0.f;
       }
+      // a compensated step of a zero term is not a no-op (it can fold the
+      // correction in early): slots past the row end are skipped there
       #pragma unroll
       for (int u = 0; u < 4; u++)
         #pragma unroll
         for (int j = 0; j < NV; j++)
           #pragma unroll
           for (int i = 0; i < V; i++) {
-            if (KAHAN) kahan_fma(acc.v[j][i], comp.v[j][i], v[u], b[u][j][i]);
-            else acc.v[j][i] = fmaf(v[u], b[u][j][i], acc.v[j][i]);
+            if (KAHAN) {
+              if (q + u < cnt) kahan_fma(acc.v[j][i], comp.v[j][i], v[u], b[u][j][i]);
+            } else {
+              acc.v[j][i] = fmaf(v[u], b[u][j][i], acc.v[j][i]);
+            }
           }
     }
   }
@@ -237,8 +242,11 @@ __device__ __forceinline__ void rbpr_slot(const RbArgs &a, int s, int e, int slo
       for (int j = 0; j < NV; j++)
         #pragma unroll
         for (int i = 0; i < V; i++) {
-          if (KAHAN) kahan_fma(acc.v[j][i], comp.v[j][i], v[u], b[u][j][i]);
-          else acc.v[j][i] = fmaf(v[u], b[u][j][i], acc.v[j][i]);
+          if (KAHAN) {
+            if (p0 + u * S < e) kahan_fma(acc.v[j][i], comp.v[j][i], v[u], b[u][j][i]);  // not past the row
+          } else {
+            acc.v[j][i] = fmaf(v[u], b[u][j][i], acc.v[j][i]);
+          }
         }
   }
 }
