@@ -16,7 +16,8 @@
 //   3. bucket_partition_kernel: a tile of TB_E nonzeros finds the row of
 //      each nonzero (the rows starting inside the tile are marked in shared
 //      memory and a block max-scan spreads them), reserves one range per
-//      bucket it touches and writes (position, row, column) records there;
+//      bucket it touches, groups its (position, row, column) records by
+//      bucket in shared memory and writes each group as one contiguous run;
 //   4. bucket_sort_kernel: a block per bucket counts its columns in shared
 //      memory (writing t_indptr), places the records by column and sorts
 //      each column by position (insertion sort up to 32 entries, bitonic
@@ -333,7 +334,7 @@ static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out
 // Two-level bucket transpose (ss_csr_transpose)
 // ---------------------------------------------------------------------
 constexpr int TB_T = 1024;            // threads per block (count, scan)
-constexpr int TB_PT = 512;            // threads per block (partition; two blocks per SM)
+constexpr int TB_PT = 1024;           // threads per block (partition)
 constexpr int TB_PER = 8;             // nonzeros per thread in a partition tile
 constexpr int TB_E = TB_PT * TB_PER;  // nonzeros per partition tile
 constexpr int TB_ST = 512;            // threads per block (bucket sort; two blocks per SM)
@@ -524,13 +525,19 @@ struct PartArgs {
   int32_t *cursor, *pos, *row, *col;
 };
 
-// One tile of TB_E nonzeros per round: rows, then (position, row, column)
-// records into the tile's reserved range of each bucket.
-__global__ void __launch_bounds__(TB_PT, 2) bucket_partition_kernel(PartArgs a) {
+// One tile of TB_E nonzeros per round: the row of each nonzero, then the
+// tile's (position, row, column) records grouped by bucket in shared memory
+// (a counting sort of the tile) and written out as one contiguous run per
+// bucket into the range the tile reserved there, so that consecutive
+// threads store consecutive addresses.
+__global__ void __launch_bounds__(TB_PT, 1) bucket_partition_kernel(PartArgs a) {
   extern __shared__ int32_t sm[];
-  int32_t *hist = sm;             // [NB]
-  int32_t *base = hist + a.NB;    // [NB]
-  int32_t *rows = base + a.NB;    // [TB_E]
+  int32_t *lst = sm;               // [NB + 1]: the tile's count per bucket, then its start in the tile
+  int32_t *cur = lst + a.NB + 1;   // [NB]: placement cursors
+  int32_t *base = cur + a.NB;      // [NB]: the tile's range in each bucket
+  int32_t *rows = base + a.NB;     // [TB_E]: rows (marks, running maximum); then the staged rows
+  int32_t *s_pos = rows + TB_E;    // [TB_E]: staged positions
+  int32_t *s_col = s_pos + TB_E;   // [TB_E]: staged columns
   __shared__ int32_t wbuf[33];
   __shared__ int32_t r01[2];
   const int tid = threadIdx.x;
@@ -541,7 +548,7 @@ __global__ void __launch_bounds__(TB_PT, 2) bucket_partition_kernel(PartArgs a) 
       const int r = warp_row_of(a.indptr, a.M, tid < 32 ? b0 : b0 + n - 1, tid & 31);
       if ((tid & 31) == 0) r01[tid >> 5] = r;
     }
-    for (int i = tid; i < a.NB; i += TB_PT) hist[i] = 0;
+    for (int i = tid; i < a.NB; i += TB_PT) lst[i] = 0;
     int c[TB_PER], rr[TB_PER];
     #pragma unroll
     for (int k = 0; k < TB_PER; k++) {
@@ -581,25 +588,36 @@ __global__ void __launch_bounds__(TB_PT, 2) bucket_partition_kernel(PartArgs a) 
     }
     #pragma unroll
     for (int k = 0; k < TB_PER; k++)
-      if ((unsigned)c[k] < (unsigned)a.K) atomicAdd(hist + (c[k] >> a.f), 1);
-    __syncthreads();
+      if ((unsigned)c[k] < (unsigned)a.K) atomicAdd(lst + (c[k] >> a.f), 1);
+    __syncthreads();  // counts complete; rows read into registers
+    // the tile's range in each bucket it touches
     for (int i = tid; i < a.NB; i += TB_PT) {
-      const int h = hist[i];
+      const int h = lst[i];
       base[i] = h ? atomicAdd(a.cursor + i, h) : 0;
-      hist[i] = 0;
     }
+    const int valid = block_scan<false>(lst, a.NB, wbuf);  // lst: each bucket's start in the tile
+    for (int i = tid; i < a.NB; i += TB_PT) cur[i] = lst[i];
+    if (tid == 0) lst[a.NB] = valid;
     __syncthreads();
     #pragma unroll
     for (int k = 0; k < TB_PER; k++) {
       if ((unsigned)c[k] < (unsigned)a.K) {
-        const int bk = c[k] >> a.f;
-        const int q = base[bk] + atomicAdd(hist + bk, 1);
-        a.pos[q] = b0 + tid + k * TB_PT;
-        a.row[q] = rr[k];
-        a.col[q] = c[k];
+        const int q = atomicAdd(cur + (c[k] >> a.f), 1);
+        s_pos[q] = b0 + tid + k * TB_PT;
+        rows[q] = rr[k];
+        s_col[q] = c[k];
       }
     }
-    __syncthreads();  // the next tile reuses hist, base and rows
+    __syncthreads();
+    for (int i = tid; i < valid; i += TB_PT) {
+      const int col = s_col[i];
+      const int bk = col >> a.f;
+      const int q = base[bk] + (i - lst[bk]);
+      a.pos[q] = s_pos[i];
+      a.row[q] = rows[i];
+      a.col[q] = col;
+    }
+    __syncthreads();  // the next tile reuses the shared arrays
   }
 }
 
@@ -754,7 +772,7 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   cudaError_t e = cudaMemsetAsync(w.count, 0, (size_t)pl.NB * 4, s);
   if (e != cudaSuccess) return cuda_fail(e, "transpose clear");
   const size_t hist_smem = (size_t)pl.NB * 4;
-  const size_t part_smem = (size_t)(2 * pl.NB + TB_E) * 4;
+  const size_t part_smem = (size_t)(3 * pl.NB + 1 + 3 * TB_E) * 4;
   const size_t sort_smem = (size_t)(2 * pl.F + 1 + 64 + 2 * pl.cap) * 4;
   e = cudaFuncSetAttribute(bucket_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem);
   if (e == cudaSuccess)
@@ -770,7 +788,7 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   pa.indptr = A->indptr; pa.cols = A->indices;
   pa.M = M; pa.K = K; pa.nnz = nnz; pa.f = pl.f; pa.NB = pl.NB;
   pa.cursor = w.cursor; pa.pos = w.pos; pa.row = w.row; pa.col = w.col;
-  bucket_partition_kernel<<<(int)std::min<long long>(tiles, 2LL * sms), TB_PT, part_smem, s>>>(pa);
+  bucket_partition_kernel<<<(int)std::min<long long>(tiles, sms), TB_PT, part_smem, s>>>(pa);
   SortArgs sa;
   sa.start = w.start; sa.pos = w.pos; sa.row = w.row; sa.col = w.col;
   sa.K = K; sa.NB = pl.NB; sa.f = pl.f; sa.F = pl.F; sa.cap = pl.cap;
