@@ -1,10 +1,7 @@
-// Launchers of the sequential-walk kernels (templates in eb_walk.cuh and
-// eb_g4.cuh).
-#include <cudaTypedefs.h>
-
+// Launchers of the sequential-walk kernels (templates in eb_walk.cuh).
 #include <mutex>
 
-#include "eb_g4.cuh"
+#include "eb_walk.cuh"
 
 namespace ss {
 
@@ -58,52 +55,6 @@ static ss_status run_sr(void *fn, void *arg, const EbGeom &g, size_t smem, cudaS
 
 static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
-// cuTensorMapEncodeTiled, looked up once through the runtime (no link to the
-// driver library); null when the driver does not provide it.
-static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static std::once_flag once;
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  std::call_once(once, [] {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
-}
-
-// The gather walk takes B rows by tensor copies: a lane's share of a row is
-// one or two 16-byte vectors, B and its rows 16-byte aligned, a box of the
-// column tile (<= 256 elements), and a tensor map the driver accepts.
-static bool g4_tensor_map(const SpmmCall &c, const EbGeom &g, CUtensorMap *m) {
-  const int es = dtype_size(c.val_dtype);
-  if (g.cs.lanes < 2 || g.cs.V * es != 16 || (g.cs.NV != 1 && g.cs.NV != 2) || g.cs.col_tile > 256) return false;
-  if (!aligned16(c.B) || ((size_t)c.N * es) % 16 != 0 || c.K < 1 || g.stage > 64) return false;
-  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-  if (!enc) return false;
-  const CUtensorMapDataType dt = c.val_dtype == SS_F32    ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                 : c.val_dtype == SS_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
-                                                          : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
-  const cuuint64_t dims[2] = {(cuuint64_t)c.N, (cuuint64_t)c.K};
-  const cuuint64_t strides[1] = {(cuuint64_t)c.N * (cuuint64_t)es};
-  const cuuint32_t box[2] = {(cuuint32_t)g.cs.col_tile, 1};
-  const cuuint32_t estr[2] = {1, 1};
-  // L2 fetches no wider than a gathered row: neighbouring rows are not wanted
-  const int row = g.cs.col_tile * es;
-  const CUtensorMapL2promotion promo = row >= 256   ? CU_TENSOR_MAP_L2_PROMOTION_L2_256B
-                                       : row >= 128 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B
-                                                    : CU_TENSOR_MAP_L2_PROMOTION_NONE;
-  return enc(m, dt, 2, const_cast<void *>(c.B), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-             CU_TENSOR_MAP_SWIZZLE_NONE, promo, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-static void *g4_kernel(const SpmmCall &c, const EbGeom &g) {
-  if (c.val_dtype == SS_F32) return g4_kernel_f32(g.cs.V, g.cs.NV, c.c_dtype);
-  if (c.val_dtype == SS_BF16) return g4_kernel_bf16(g.cs.V, g.cs.NV, c.c_dtype == SS_F32);
-  return g4_kernel_f16(g.cs.V, g.cs.NV, c.c_dtype == SS_F32);
-}
-
 ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t s) {
   EbArgs a = eb_base_args(g, ws, c.N);
   a.M = c.M; a.K = c.K; a.nnz = c.nnz;
@@ -127,15 +78,6 @@ ss_status launch_ebsr(const SpmmCall &c, const EbGeom &g, void *ws, cudaStream_t
   if (g.cs.lanes == 1) {
     void *nf = narrow_kernel(c.val_dtype, c.c_dtype, g.cs.V, g.cs.NV);
     if (nf) return run_sr(nf, &a, g, 0, s, "ebsr narrow launch");
-  }
-  // B rows by tensor gathers into a shared-memory ring where the shapes allow
-  G4Args p;
-  void *gf = g4_kernel(c, g);
-  const size_t g4_smem =
-      (size_t)g.workers_per_block * g4_worker_bytes(g.stage, dtype_size(c.val_dtype), g.cs.col_tile);
-  if (gf && g4_smem <= (size_t)max_smem_per_block() && g4_tensor_map(c, g, &p.tmap)) {
-    p.a = a;
-    return run_sr(gf, &p, g, g4_smem, s, "ebsr gather launch");
   }
   return run_sr(fn, &a, g, sr_smem_bytes(g.stage, g.workers_per_block, dtype_size(c.val_dtype)), s, "ebsr launch");
 }

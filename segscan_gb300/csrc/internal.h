@@ -100,8 +100,6 @@ int *walk_error_ptr();
 // streaming multiprocessors of the current device, looked up once per device
 // (util.cu); 1 when the query fails
 int sm_count();
-// Dynamic shared memory a block may opt into on the current device.
-int max_smem_per_block();
 
 // Launchers (kernels live in spmm_rb.cu, eb_walk.cu, eb_scan.cu).
 ss_status launch_rbsr(const SpmmCall &c, const RbGeom &g, cudaStream_t s);

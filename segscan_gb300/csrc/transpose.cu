@@ -399,32 +399,37 @@ static size_t bucket_ws_bytes(const BucketPlan &p, int nnz, BucketWs *w, void *b
   return o;
 }
 
-// Scan of x[0, n) in place by the whole block, each thread owning a
-// contiguous run of ceil(n / blockDim.x) entries: exclusive prefix sums
-// (MAX false) or inclusive prefix maxima (MAX true).  Returns the sum / the
-// maximum to every thread.  wbuf: 33 ints of shared memory.
+// Scan of x[0, n) in place by the whole block: exclusive prefix sums (MAX
+// false) or inclusive prefix maxima (MAX true).  Each warp owns a contiguous
+// segment and scans it 32 consecutive entries at a time with shuffles (no
+// shared-memory bank conflicts), then the warps' totals are scanned and
+// applied.  Returns the sum / the maximum to every thread.  wbuf: 33 ints of
+// shared memory.
 template <bool MAX>
 __device__ int block_scan(int32_t *x, int n, int32_t *wbuf) {
   constexpr int ID = MAX ? INT_MIN : 0;
   auto op = [](int u, int v) { return MAX ? max(u, v) : u + v; };
-  const int T = blockDim.x, tid = threadIdx.x;
-  const int per = (n + T - 1) / T;
-  const int lo = min(tid * per, n), hi = min(lo + per, n);
-  int t = ID;
-  for (int i = lo; i < hi; i++) t = op(t, x[i]);
-  const int lane = tid & 31, wid = tid >> 5;
-  int incl = t;
-  #pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, incl, off);
-    if (lane >= off) incl = op(incl, y);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, W = blockDim.x >> 5;
+  const int seg = ((n + W - 1) / W + 31) & ~31;  // entries per warp, a multiple of 32
+  const int lo = min(wid * seg, n), hi = min(lo + seg, n);
+  int carry = ID;
+  for (int base = lo; base < hi; base += 32) {
+    const int i = base + lane;
+    const int v0 = i < hi ? x[i] : ID;
+    int v = v0;
+    #pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, v, off);
+      if (lane >= off) v = op(v, y);
+    }
+    v = op(carry, v);  // inclusive within the warp's segment
+    if (i < hi) x[i] = MAX ? v : v - v0;
+    carry = __shfl_sync(0xffffffffu, v, 31);
   }
-  int excl = __shfl_up_sync(0xffffffffu, incl, 1);
-  if (lane == 0) excl = ID;
-  if (lane == 31) wbuf[wid] = incl;
+  if (lane == 0) wbuf[wid] = carry;
   __syncthreads();
   if (wid == 0) {
-    const int w = lane < (T >> 5) ? wbuf[lane] : ID;
+    const int w = lane < W ? wbuf[lane] : ID;
     int wi = w;
     #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
@@ -433,21 +438,13 @@ __device__ int block_scan(int32_t *x, int n, int32_t *wbuf) {
     }
     int we = __shfl_up_sync(0xffffffffu, wi, 1);
     if (lane == 0) we = ID;
-    wbuf[lane] = we;  // exclusive prefix of the warp totals
+    wbuf[lane] = we;  // what the warps before each one contribute
     if (lane == 31) wbuf[32] = wi;
   }
   __syncthreads();
-  int run = op(wbuf[wid], excl);
-  for (int i = lo; i < hi; i++) {
-    const int v = x[i];
-    if (MAX) {
-      run = max(run, v);
-      x[i] = run;
-    } else {
-      x[i] = run;
-      run += v;
-    }
-  }
+  const int pre = wbuf[wid];
+  if (wid > 0)
+    for (int i = lo + lane; i < hi; i += 32) x[i] = op(pre, x[i]);
   const int total = wbuf[32];
   __syncthreads();
   return total;
