@@ -337,11 +337,11 @@ constexpr int TB_T = 1024;            // threads per block (count, scan)
 constexpr int TB_PT = 1024;           // threads per block (partition)
 constexpr int TB_PER = 8;             // nonzeros per thread in a partition tile
 constexpr int TB_E = TB_PT * TB_PER;  // nonzeros per partition tile
-constexpr int TB_ST = 512;            // threads per block (bucket sort; two blocks per SM)
+constexpr int TB_ST = 1024;           // threads per block (bucket sort; one block per SM)
 constexpr int TB_F_LOG2_MAX = 13;  // at most 8192 columns per bucket
 constexpr int TB_NB_MAX = 8192;    // buckets
 #ifndef SS_TB_SORT_SMEM_KB
-#define SS_TB_SORT_SMEM_KB 110
+#define SS_TB_SORT_SMEM_KB 220
 #endif
 constexpr int TB_SORT_SMEM = SS_TB_SORT_SMEM_KB * 1024;
 constexpr int TB_LONG = 40;  // slot of the long-column count in the sort block's scratch
@@ -351,8 +351,12 @@ struct BucketPlan {
   int f, F, NB, cap;   // F = 2^f columns per bucket; cap = records a sort block holds
 };
 
-// Records a sort block holds beside its 2F + 1 counters and 64 ints of scratch.
-static int sort_cap(int F) { return (TB_SORT_SMEM - (2 * F + 1 + 64) * 4) / 8; }
+// Records a sort block holds (a multiple of 4): each takes five ints (the
+// three staged record arrays, the two placed ones) beside the mbarrier (4
+// ints), eight ints of alignment slack per staged array, 2F + 1 counters and
+// 64 ints of scratch.
+static int sort_bytes(int F, int cap) { return (4 + 3 * (cap + 8) + 2 * cap + 2 * F + 1 + 64) * 4; }
+static int sort_cap(int F) { return ((TB_SORT_SMEM - sort_bytes(F, 0)) / 20) & ~3; }
 
 static BucketPlan bucket_plan(int K, int nnz) {
   BucketPlan p;
@@ -384,9 +388,10 @@ static size_t bucket_ws_bytes(const BucketPlan &p, int nnz, BucketWs *w, void *b
   const size_t count = o; o += align256((size_t)(p.NB + 1) * 4);
   const size_t start = o; o += align256((size_t)(p.NB + 1) * 4);
   const size_t cursor = o; o += align256((size_t)(p.NB + 1) * 4);
-  const size_t pos = o; o += align256((size_t)nnz * 4);
-  const size_t row = o; o += align256((size_t)nnz * 4);
-  const size_t col = o; o += align256((size_t)nnz * 4);
+  // four spare entries each: a sort block reads whole 16-byte words
+  const size_t pos = o; o += align256((size_t)(nnz + 4) * 4);
+  const size_t row = o; o += align256((size_t)(nnz + 4) * 4);
+  const size_t col = o; o += align256((size_t)(nnz + 4) * 4);
   if (w) {
     char *b = (char *)base;
     w->count = (int32_t *)(b + count);
@@ -654,33 +659,105 @@ struct SortArgs {
   const void *vals;  // A's values, or null: no value gather
   void *t_vals;
   int vsize;         // 4 or 2 bytes
+  int *err;          // device status word for the bounded waits
 };
 
-__global__ void __launch_bounds__(TB_ST, 2) bucket_sort_kernel(SortArgs a) {
-  extern __shared__ int32_t sm[];
-  int32_t *cnt = sm;                 // [F + 1]: counts, then column starts
-  int32_t *cur = cnt + a.F + 1;      // [F]: placement cursors, then the long columns
-  int32_t *wbuf = cur + a.F;         // [64]: scan scratch; [TB_LONG]: long-column count
-  int32_t *sp = wbuf + 64;           // [cap] positions
-  int32_t *sr = sp + a.cap;          // [cap] rows
+constexpr uint32_t TB_SPIN_LIMIT = 1u << 22;  // mbarrier polls before giving up
+
+// The records of bucket b into the staging arrays: one bulk copy per array
+// from the 16-byte word holding its first record to the one holding its
+// last, completing on bar.  Returns the offset of the first record in the
+// staged arrays (0..3).  Thread 0 only.
+__device__ __forceinline__ int stage_bucket(const SortArgs &a, int b, int32_t *rc, int32_t *rp, int32_t *rr,
+                                            uint64_t *bar) {
+  const int s0 = __ldg(a.start + b), n = __ldg(a.start + b + 1) - s0;
+  const int w0 = s0 & ~3, w1 = (s0 + n + 3) & ~3;
+  const uint32_t bytes = (uint32_t)(w1 - w0) * 4u;
+  fence_async_smem();
+  mbar_expect_tx(bar, 3u * bytes);
+  bulk_g2s(rc, a.col + w0, bytes, bar);
+  bulk_g2s(rp, a.pos + w0, bytes, bar);
+  bulk_g2s(rr, a.row + w0, bytes, bar);
+  return s0 - w0;
+}
+
+// A bucket per round, one block per SM.  A bucket that fits the record store
+// arrives by bulk copies (the next one's issued as soon as this one's
+// records are placed, so it lands while this one is sorted and written); its
+// columns are counted, its records placed by column and sorted inside each
+// column, all in shared memory.  A larger bucket is placed and sorted in
+// the output arrays.
+__global__ void __launch_bounds__(TB_ST, 1) bucket_sort_kernel(SortArgs a) {
+  extern __shared__ __align__(16) int32_t sm[];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm);  // [4 ints]
+  const int stg = a.cap + 8;          // staged array length (alignment slack; a multiple of 4)
+  int32_t *rc = sm + 4;               // [stg] staged columns
+  int32_t *rp = rc + stg;             // [stg] staged positions
+  int32_t *rr = rp + stg;             // [stg] staged rows
+  int32_t *sp = rr + stg;             // [cap] placed positions
+  int32_t *sr = sp + a.cap;           // [cap] placed rows
+  int32_t *cnt = sr + a.cap;          // [F + 1]: counts, then column starts
+  int32_t *cur = cnt + a.F + 1;       // [F]: placement cursors, then the long columns
+  int32_t *wbuf = cur + a.F;          // [64]: scan scratch; [TB_LONG]: long-column count; [48]: staged offset
   const int tid = threadIdx.x;
+  uint32_t phase = 0;
+  // bucket b arrives by bulk copies: not empty, and it fits the record store
+  auto fits_at = [&](int b) {
+    if (b >= a.NB) return false;
+    const int n = __ldg(a.start + b + 1) - __ldg(a.start + b);
+    return n > 0 && n <= a.cap;
+  };
+  auto wait_staged = [&]() -> bool {
+    for (uint32_t it = 0; it < TB_SPIN_LIMIT; it++)
+      if (mbar_try_wait(bar, phase)) return true;
+    return false;
+  };
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (fits_at(blockIdx.x)) wbuf[48] = stage_bucket(a, blockIdx.x, rc, rp, rr, bar);
+  }
+  __syncthreads();
   for (int b = blockIdx.x; b < a.NB; b += gridDim.x) {
     const int c0 = b << a.f;
     const int nf = min(a.F, a.K - c0);
     const int s0 = __ldg(a.start + b), n = __ldg(a.start + b + 1) - s0;
+    const bool fits = n <= a.cap;
+    const bool staged = n > 0 && fits;
     for (int i = tid; i < nf; i += TB_ST) cnt[i] = 0;
     if (tid == 0) wbuf[TB_LONG] = 0;
-    __syncthreads();
-    for (int i0 = 0; i0 < n; i0 += 4 * TB_ST) {
-      int c[4];
-      #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int i = i0 + tid + u * TB_ST;
-        c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
+    int d = 0;  // first staged record
+    if (staged) {
+      if (!__syncthreads_and(wait_staged())) {
+        // the copies did not land: record it, wait (bounded) once more for
+        // them, and stop; no other copy of this block is in flight
+        if (tid == 0 && a.err) atomicExch(a.err, (int)SS_ERR_TIMEOUT);
+        wait_staged();
+        return;
       }
-      #pragma unroll
-      for (int u = 0; u < 4; u++)
-        if ((unsigned)c[u] < (unsigned)nf) atomicAdd(cnt + c[u], 1);
+      phase ^= 1u;
+      d = wbuf[48];
+    } else {
+      __syncthreads();
+    }
+    // count the bucket's columns
+    if (fits) {
+      for (int i = tid; i < n; i += TB_ST) {
+        const int c = rc[d + i] - c0;
+        if ((unsigned)c < (unsigned)nf) atomicAdd(cnt + c, 1);
+      }
+    } else {
+      for (int i0 = 0; i0 < n; i0 += 4 * TB_ST) {
+        int c[4];
+        #pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int i = i0 + tid + u * TB_ST;
+          c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
+        }
+        #pragma unroll
+        for (int u = 0; u < 4; u++)
+          if ((unsigned)c[u] < (unsigned)nf) atomicAdd(cnt + c[u], 1);
+      }
     }
     __syncthreads();
     const int total = block_scan<false>(cnt, nf, wbuf);
@@ -690,30 +767,43 @@ __global__ void __launch_bounds__(TB_ST, 2) bucket_sort_kernel(SortArgs a) {
     }
     if (tid == 0) cnt[nf] = total;
     __syncthreads();
-    // place the records by column: in shared memory, or straight into the
-    // outputs when the bucket is larger than the record store
-    const bool fits = n <= a.cap;
     int32_t *dp = fits ? sp : a.perm + s0;
     int32_t *dr = fits ? sr : a.t_indices + s0;
-    for (int i0 = 0; i0 < n; i0 += 4 * TB_ST) {
-      int c[4], p[4], r[4];
-      #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int i = i0 + tid + u * TB_ST;
-        c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
-        p[u] = i < n ? __ldg(a.pos + s0 + i) : 0;
-        r[u] = i < n ? __ldg(a.row + s0 + i) : 0;
-      }
-      #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        if ((unsigned)c[u] < (unsigned)nf) {
-          const int q = atomicAdd(cur + c[u], 1);
-          dp[q] = p[u];
-          dr[q] = r[u];
+    if (fits) {
+      for (int i = tid; i < n; i += TB_ST) {
+        const int c = rc[d + i] - c0;
+        if ((unsigned)c < (unsigned)nf) {
+          const int q = atomicAdd(cur + c, 1);
+          dp[q] = rp[d + i];
+          dr[q] = rr[d + i];
         }
       }
+      __syncthreads();
+      // the staged arrays are free: the next bucket of this block streams in
+      if (tid == 0 && fits_at(b + gridDim.x)) wbuf[48] = stage_bucket(a, b + gridDim.x, rc, rp, rr, bar);
+    } else {
+      for (int i0 = 0; i0 < n; i0 += 4 * TB_ST) {
+        int c[4], p[4], r[4];
+        #pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int i = i0 + tid + u * TB_ST;
+          c[u] = i < n ? __ldg(a.col + s0 + i) - c0 : -1;
+          p[u] = i < n ? __ldg(a.pos + s0 + i) : 0;
+          r[u] = i < n ? __ldg(a.row + s0 + i) : 0;
+        }
+        #pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if ((unsigned)c[u] < (unsigned)nf) {
+            const int q = atomicAdd(cur + c[u], 1);
+            dp[q] = p[u];
+            dr[q] = r[u];
+          }
+        }
+      }
+      __syncthreads();
+      // this bucket used no staging; the next one, if it fits, is staged now
+      if (tid == 0 && fits_at(b + gridDim.x)) wbuf[48] = stage_bucket(a, b + gridDim.x, rc, rp, rr, bar);
     }
-    __syncthreads();
     // each column by position: short ones by a thread, long ones by the block
     for (int i = tid; i < nf; i += TB_ST) {
       const int s = cnt[i], len = cnt[i + 1] - s;
@@ -729,8 +819,8 @@ __global__ void __launch_bounds__(TB_ST, 2) bucket_sort_kernel(SortArgs a) {
         bitonic_block(sp + s, len);
         bitonic_block(sr + s, len);
       } else {
-        sort_segment(dp + s, len, sp, a.cap);
-        sort_segment(dr + s, len, sp, a.cap);
+        sort_segment(dp + s, len, sp, 2 * a.cap);
+        sort_segment(dr + s, len, sp, 2 * a.cap);
       }
     }
     if (fits) {
@@ -770,7 +860,7 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   if (e != cudaSuccess) return cuda_fail(e, "transpose clear");
   const size_t hist_smem = (size_t)pl.NB * 4;
   const size_t part_smem = (size_t)(3 * pl.NB + 1 + 3 * TB_E) * 4;
-  const size_t sort_smem = (size_t)(2 * pl.F + 1 + 64 + 2 * pl.cap) * 4;
+  const size_t sort_smem = (size_t)sort_bytes(pl.F, pl.cap);
   e = cudaFuncSetAttribute(bucket_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(bucket_partition_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)part_smem);
@@ -793,7 +883,8 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   sa.vals = t_vals ? A->values : nullptr;
   sa.t_vals = t_vals;
   sa.vsize = dtype_size(A->value_dtype);
-  bucket_sort_kernel<<<std::min(pl.NB, 2 * sms), TB_ST, sort_smem, s>>>(sa);
+  sa.err = walk_error_ptr();
+  bucket_sort_kernel<<<std::min(pl.NB, sms), TB_ST, sort_smem, s>>>(sa);
   e = cudaGetLastError();
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
 }
