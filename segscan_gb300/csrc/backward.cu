@@ -8,15 +8,21 @@
 // so one gather of the dC row serves both gradients: SDDMM followed by
 // A^T * dC would gather a B row and then a dC row for every nonzero.
 //
-// A group of L lanes along N owns a row of A^T (lane l holds elements
-// (j * L + l) * V .. + V - 1 for j < NV, so each gathered row is one
-// contiguous request per j), keeps that row of B in registers, and walks
-// the row's nonzeros four at a time with their four dC rows in flight.
-// The four partial dot products are reduced across the lanes by a fixed
-// butterfly (butterfly_sum); dB is summed in position order, with Kahan
-// compensation when the row is longer than the threshold, so dB has the
-// bits of the row-balanced sequential SpMM (rbsr) on A^T.  FP32 math.
+// A group of L lanes along N (lane l holds elements (j * L + l) * V .. + V -
+// 1 for j < NV, so each gathered row is one contiguous request per j) owns a
+// contiguous block of A^T rows: the rows that start inside its share of
+// about nnz / groups positions, so the blocks hold similar numbers of
+// nonzeros and no row is split.  It streams the block's nonzeros in order,
+// four at a time, with their four dC rows and values in flight while the
+// next four positions' indices and permutation entries load.  Row ends come
+// from a window of t_indptr the lanes hold one entry each, and the B slice
+// of the next row is loaded one row ahead, so a row change costs no round
+// trip.  The four partial dot products are reduced across the lanes by a
+// fixed butterfly (butterfly_sum); dB is summed in position order, with
+// Kahan compensation when the row is longer than the threshold, so dB has
+// the bits of the row-balanced sequential SpMM (rbsr) on A^T.  FP32 math.
 #include "common.cuh"
+#include "eb_common.cuh"
 #include "internal.h"
 
 namespace ss {
@@ -25,6 +31,8 @@ constexpr int BWD_U = 4;  // nonzeros (dC rows) in flight per group
 
 struct BwdArgs {
   int K, M, N, nnz, kahan;
+  int chunk;        // positions per group's share
+  int groups;       // groups with a share (the last one takes the rest)
   const int32_t *t_indptr, *t_indices, *perm;
   const void *vals;  // A's values in A's order, or null (ones)
   const float *dC;   // [M x N]
@@ -40,81 +48,133 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
   const int L = a.lanes;
   const int lane = tid & (L - 1);
   const int group = (blockIdx.x * blockDim.x + tid) >> a.log2_lanes;
-  const int groups = (gridDim.x * blockDim.x) >> a.log2_lanes;
   const unsigned wl = tid & 31;
   const unsigned mask = L >= 32 ? 0xffffffffu : (((1u << L) - 1u) << (wl & ~(unsigned)(L - 1)));
+  if (group >= a.groups) return;  // whole groups exit together
   const uint64_t keep = policy_keep(1.0f), strm = policy_stream();
   const T *B = (const T *)a.B;
   const T *vals = (const T *)a.vals;
   bool act[NV];
   #pragma unroll
   for (int j = 0; j < NV; j++) act[j] = (j * L + lane) * V < a.N;
-  for (int k = group; k < a.K; k += groups) {
-    const int s = __ldg(a.t_indptr + k), e = __ldg(a.t_indptr + k + 1);
-    const bool kahan = e - s > a.kahan;
-    float b[NV][V], acc[NV][V], comp[NV][V];
+  // the rows starting in [lo, hi)
+  const long long lo = (long long)group * a.chunk;
+  const int r_lo = group_lower_bound(a.t_indptr, a.K, (int)lo, lane, L, mask);
+  const int r_hi = group == a.groups - 1
+                       ? a.K
+                       : group_lower_bound(a.t_indptr, a.K, (int)min(lo + a.chunk, (long long)a.nnz), lane, L, mask);
+  if (r_lo >= r_hi) return;
+  const int qe = __ldg(a.t_indptr + r_hi);
+
+  // t_indptr[wb + l] held by lane l
+  int wb = r_lo, win = __ldg(a.t_indptr + min(r_lo + lane, a.K));
+  auto ptr_at = [&](int r) -> int {  // t_indptr[r], r >= wb
+    if (r >= wb + L) {
+      wb = r;
+      win = __ldg(a.t_indptr + min(r + lane, a.K));
+    }
+    return __shfl_sync(mask, win, r - wb, L);
+  };
+  auto load_b = [&](int r, float (&dst)[NV][V]) {
     #pragma unroll
     for (int j = 0; j < NV; j++) {
       #pragma unroll
-      for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; b[j][i] = 0.f; }
-      if (act[j] && e > s) load_vec<T, V>(B + (int64_t)k * a.N + (j * L + lane) * V, b[j], strm);
+      for (int i = 0; i < V; i++) dst[j][i] = 0.f;
+      if (act[j] && r < r_hi) load_vec<T, V>(B + (int64_t)r * a.N + (j * L + lane) * V, dst[j], strm);
     }
-    for (int q0 = s; q0 < e; q0 += BWD_U) {
-      int row[BWD_U], pos[BWD_U];
-      float av[BWD_U];
-      float g[BWD_U][NV][V];
-      #pragma unroll
-      for (int u = 0; u < BWD_U; u++) {
-        const bool live = q0 + u < e;
-        row[u] = live ? ld_idx(a.t_indices + q0 + u, strm) : -1;
-        pos[u] = live ? ld_idx(a.perm + q0 + u, strm) : -1;
-      }
-      #pragma unroll
-      for (int u = 0; u < BWD_U; u++) {
-        const bool ok = (unsigned)row[u] < (unsigned)a.M && (unsigned)pos[u] < (unsigned)a.nnz;
-        av[u] = ok ? load_val<T>(vals, pos[u], keep) : 0.f;
-        #pragma unroll
-        for (int j = 0; j < NV; j++) {
-          if (ok && act[j]) {
-            load_vec<float, V>(a.dC + (int64_t)row[u] * a.N + (j * L + lane) * V, g[u][j], keep);
-          } else {
-            #pragma unroll
-            for (int i = 0; i < V; i++) g[u][j][i] = 0.f;
-          }
-        }
-      }
-      float part[BWD_U];
-      #pragma unroll
-      for (int u = 0; u < BWD_U; u++) {
-        part[u] = 0.f;
-        #pragma unroll
-        for (int j = 0; j < NV; j++)
-          #pragma unroll
-          for (int i = 0; i < V; i++) {
-            part[u] = fmaf(g[u][j][i], b[j][i], part[u]);
-            if (!kahan) acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
-            else if (q0 + u < e) kahan_fma(acc[j][i], comp[j][i], av[u], g[u][j][i]);  // not past the row
-          }
-      }
-      // the four dot products: reduced across the lanes, stored at A's positions
-      if (L >= BWD_U) {
-        int base = 0;
-        const float x = butterfly_sum<BWD_U>(part, lane, L, mask, base);
-        if ((lane & (L / BWD_U - 1)) == 0 && pos[base] >= 0 && pos[base] < a.nnz) a.dvals[pos[base]] = x;
-      } else {
-        #pragma unroll
-        for (int u = 0; u < BWD_U; u++) {
-          float x = part[u];
-          for (int off = L >> 1; off > 0; off >>= 1) x += __shfl_xor_sync(mask, x, off);
-          if (lane == 0 && pos[u] >= 0 && pos[u] < a.nnz) a.dvals[pos[u]] = x;
-        }
-      }
-    }
+  };
+
+  int k = r_lo;
+  int sk = ptr_at(k), ek = ptr_at(k + 1);
+  bool kahan = ek - sk > a.kahan;
+  float bcur[NV][V], bnext[NV][V], acc[NV][V], comp[NV][V];
+  load_b(k, bcur);
+  load_b(k + 1, bnext);
+  #pragma unroll
+  for (int j = 0; j < NV; j++)
+    #pragma unroll
+    for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
+  // row k is done: its dB row stored, the next row set up
+  auto next_row = [&]() {
     TC *dst = (TC *)a.dB + (int64_t)k * a.N;
     #pragma unroll
-    for (int j = 0; j < NV; j++)
+    for (int j = 0; j < NV; j++) {
       if (act[j]) store_vec<TC, V>(dst + (j * L + lane) * V, acc[j], strm);
+      #pragma unroll
+      for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; bcur[j][i] = bnext[j][i]; }
+    }
+    k++;
+    sk = ek;
+    ek = ptr_at(k + 1);
+    kahan = ek - sk > a.kahan;
+    load_b(k + 1, bnext);
+  };
+
+  int row[BWD_U], pos[BWD_U];
+  int q0 = sk;
+  #pragma unroll
+  for (int u = 0; u < BWD_U; u++) {
+    row[u] = q0 + u < qe ? ld_idx(a.t_indices + q0 + u, strm) : -1;
+    pos[u] = q0 + u < qe ? ld_idx(a.perm + q0 + u, strm) : -1;
   }
+  for (; q0 < qe; q0 += BWD_U) {
+    float av[BWD_U];
+    float g[BWD_U][NV][V];
+    #pragma unroll
+    for (int u = 0; u < BWD_U; u++) {
+      const bool ok = (unsigned)row[u] < (unsigned)a.M && (unsigned)pos[u] < (unsigned)a.nnz;
+      av[u] = ok ? load_val<T>(vals, pos[u], keep) : 0.f;
+      #pragma unroll
+      for (int j = 0; j < NV; j++) {
+        if (ok && act[j]) {
+          load_vec<float, V>(a.dC + (int64_t)row[u] * a.N + (j * L + lane) * V, g[u][j], keep);
+        } else {
+          #pragma unroll
+          for (int i = 0; i < V; i++) g[u][j][i] = 0.f;
+        }
+      }
+    }
+    // the next four positions' indices, in flight while these are used
+    int nrow[BWD_U], npos[BWD_U];
+    #pragma unroll
+    for (int u = 0; u < BWD_U; u++) {
+      const int q = q0 + BWD_U + u;
+      nrow[u] = q < qe ? ld_idx(a.t_indices + q, strm) : -1;
+      npos[u] = q < qe ? ld_idx(a.perm + q, strm) : -1;
+    }
+    float part[BWD_U];
+    #pragma unroll
+    for (int u = 0; u < BWD_U; u++) {
+      part[u] = 0.f;
+      if (q0 + u >= qe) continue;
+      while (q0 + u >= ek) next_row();  // rows that end here (empty ones too) are stored
+      #pragma unroll
+      for (int j = 0; j < NV; j++)
+        #pragma unroll
+        for (int i = 0; i < V; i++) {
+          part[u] = fmaf(g[u][j][i], bcur[j][i], part[u]);
+          if (kahan) kahan_fma(acc[j][i], comp[j][i], av[u], g[u][j][i]);
+          else acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
+        }
+    }
+    // the four dot products: reduced across the lanes, stored at A's positions
+    if (L >= BWD_U) {
+      int base = 0;
+      const float x = butterfly_sum<BWD_U>(part, lane, L, mask, base);
+      if ((lane & (L / BWD_U - 1)) == 0 && pos[base] >= 0 && pos[base] < a.nnz) a.dvals[pos[base]] = x;
+    } else {
+      #pragma unroll
+      for (int u = 0; u < BWD_U; u++) {
+        float x = part[u];
+        for (int off = L >> 1; off > 0; off >>= 1) x += __shfl_xor_sync(mask, x, off);
+        if (lane == 0 && pos[u] >= 0 && pos[u] < a.nnz) a.dvals[pos[u]] = x;
+      }
+    }
+    #pragma unroll
+    for (int u = 0; u < BWD_U; u++) { row[u] = nrow[u]; pos[u] = npos[u]; }
+  }
+  // the last row with nonzeros and the empty rows after it
+  while (k < r_hi) next_row();
 }
 
 template <typename T, typename TC>
@@ -172,11 +232,17 @@ extern "C" ss_status ss_spmm_backward(const ss_csr *AT, const int32_t *perm, con
   a.t_indptr = AT->indptr; a.t_indices = AT->indices; a.perm = perm; a.vals = values;
   a.dC = dC; a.B = B; a.dB = dB; a.dvals = dvals;
   a.lanes = lanes; a.log2_lanes = ilog2(lanes);
+  // shares of about nnz / (eight blocks per SM's groups) positions, at least 64
   const int threads = 256;
   const long long groups_per_block = threads / lanes;
-  long long blocks = ((long long)K + groups_per_block - 1) / groups_per_block;
-  const long long cap = (long long)sm_count() * 8;
-  if (blocks > cap) blocks = cap;
+  const long long target = (long long)sm_count() * 8 * groups_per_block;
+  long long chunk = ((long long)nnz + target - 1) / target;
+  if (chunk < 64) chunk = 64;
+  long long groups = ((long long)nnz + chunk - 1) / chunk;
+  if (groups < 1) groups = 1;
+  a.chunk = (int)chunk;
+  a.groups = (int)groups;
+  const long long blocks = (groups + groups_per_block - 1) / groups_per_block;
   void *args[] = {&a};
   cudaError_t e = cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, 0, (cudaStream_t)stream);
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "fused backward launch");
