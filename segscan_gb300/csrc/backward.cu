@@ -75,20 +75,24 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
     }
     return __shfl_sync(mask, win, r - wb, L);
   };
-  auto load_b = [&](int r, float (&dst)[NV][V]) {
+  // B slice of row r, kept packed: 16-bit slices are widened only when the
+  // row becomes current, so the prefetch one row ahead is not waited for
+  auto load_b = [&](int r, RawVec<T, V> (&dst)[NV]) {
     #pragma unroll
     for (int j = 0; j < NV; j++) {
-      #pragma unroll
-      for (int i = 0; i < V; i++) dst[j][i] = 0.f;
-      if (act[j] && r < r_hi) load_vec<T, V>(B + (int64_t)r * a.N + (j * L + lane) * V, dst[j], strm);
+      zero_raw(dst[j]);
+      if (act[j] && r < r_hi) load_raw<T, V>(B + (int64_t)r * a.N + (j * L + lane) * V, dst[j], strm);
     }
   };
 
   int k = r_lo;
   int sk = ptr_at(k), ek = ptr_at(k + 1);
   bool kahan = ek - sk > a.kahan;
-  float bcur[NV][V], bnext[NV][V], acc[NV][V], comp[NV][V];
-  load_b(k, bcur);
+  float bcur[NV][V], acc[NV][V], comp[NV][V];
+  RawVec<T, V> bnext[NV];
+  load_b(k, bnext);
+  #pragma unroll
+  for (int j = 0; j < NV; j++) unpack_raw(bnext[j], bcur[j]);
   load_b(k + 1, bnext);
   #pragma unroll
   for (int j = 0; j < NV; j++)
@@ -101,7 +105,8 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
     for (int j = 0; j < NV; j++) {
       if (act[j]) store_vec<TC, V>(dst + (j * L + lane) * V, acc[j], strm);
       #pragma unroll
-      for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; bcur[j][i] = bnext[j][i]; }
+      for (int i = 0; i < V; i++) { acc[j][i] = 0.f; comp[j][i] = 0.f; }
+      unpack_raw(bnext[j], bcur[j]);
     }
     k++;
     sk = ek;
@@ -120,10 +125,14 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
   for (; q0 < qe; q0 += BWD_U) {
     float av[BWD_U];
     float g[BWD_U][NV][V];
+    RawVec<T, 1> araw[BWD_U];  // values loaded packed: widened after every gather is issued
+    bool okv[BWD_U];
     #pragma unroll
     for (int u = 0; u < BWD_U; u++) {
       const bool ok = (unsigned)row[u] < (unsigned)a.M && (unsigned)pos[u] < (unsigned)a.nnz;
-      av[u] = ok ? load_val<T>(vals, pos[u], keep) : 0.f;
+      okv[u] = ok;
+      zero_raw(araw[u]);
+      if (ok && vals) load_raw<T, 1>(vals + pos[u], araw[u], keep);
       #pragma unroll
       for (int j = 0; j < NV; j++) {
         if (ok && act[j]) {
@@ -133,6 +142,12 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
           for (int i = 0; i < V; i++) g[u][j][i] = 0.f;
         }
       }
+    }
+    #pragma unroll
+    for (int u = 0; u < BWD_U; u++) {
+      float x[1];
+      unpack_raw(araw[u], x);
+      av[u] = okv[u] ? (vals ? x[0] : 1.f) : 0.f;
     }
     // the next four positions' indices, in flight while these are used
     int nrow[BWD_U], npos[BWD_U];

@@ -145,6 +145,52 @@ __device__ __forceinline__ void load_vec(const T *p, float (&out)[V], uint64_t p
   }
 }
 
+// V elements of T (V * sizeof(T) <= 16 bytes) as raw 32-bit words: a
+// prefetch held in this form is not widened on arrival, so the thread does
+// not wait for the load until the words are unpacked.
+template <typename T, int V>
+struct RawVec {
+  static_assert(V * sizeof(T) <= 16, "one access of at most 16 bytes");
+  uint32_t w[(V * sizeof(T) + 3) / 4];
+};
+
+template <typename T, int V>
+__device__ __forceinline__ void zero_raw(RawVec<T, V> &r) {
+  #pragma unroll
+  for (int i = 0; i < (int)(sizeof(r.w) / 4); i++) r.w[i] = 0u;
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void load_raw(const T *p, RawVec<T, V> &r, uint64_t pol) {
+  constexpr int bytes = V * (int)sizeof(T);
+  if constexpr (bytes == 16) {
+    const uint4 u = ld_u128(p, pol);
+    r.w[0] = u.x; r.w[1] = u.y; r.w[2] = u.z; r.w[3] = u.w;
+  } else if constexpr (bytes == 8) {
+    const uint2 u = ld_u64(p, pol);
+    r.w[0] = u.x; r.w[1] = u.y;
+  } else if constexpr (bytes == 4) {
+    r.w[0] = ld_u32(p, pol);
+  } else {
+    r.w[0] = ld_u16(p, pol);
+  }
+}
+
+// Widens raw words to FP32 (all-zero words give +0 for every storage type).
+template <typename T, int V>
+__device__ __forceinline__ void unpack_raw(const RawVec<T, V> &r, float (&out)[V]) {
+  if constexpr (sizeof(T) == 4) {
+    #pragma unroll
+    for (int i = 0; i < V; i++) out[i] = __uint_as_float(r.w[i]);
+  } else if constexpr (V == 1) {
+    const uint16_t h = (uint16_t)r.w[0];
+    out[0] = Elem<T>::to_f(*reinterpret_cast<const T *>(&h));
+  } else {
+    #pragma unroll
+    for (int i = 0; i < V / 2; i++) unpack2(r.w[i], out[2 * i], out[2 * i + 1], (T *)nullptr);
+  }
+}
+
 // One scalar value of A (values == nullptr means 1, the reference's
 // __guard_load_default_one, test-cg/include/util/check.cuh:104-111).
 template <typename T>
