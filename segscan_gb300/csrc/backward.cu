@@ -42,14 +42,17 @@ struct BwdArgs {
   int lanes, log2_lanes;
 };
 
-template <typename T, typename TC, int V, int NV>
-__global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
+// WARP: the group is a whole warp (32 lanes), so lane masks and shuffle
+// widths are compile-time constants and warp collectives need no
+// convergence handling.
+template <typename T, typename TC, int V, int NV, bool WARP>
+__global__ void __launch_bounds__(256, NV == 1 ? 4 : 1) fused_bwd_kernel(BwdArgs a) {
   const int tid = threadIdx.x;
-  const int L = a.lanes;
+  const int L = WARP ? 32 : a.lanes;
   const int lane = tid & (L - 1);
-  const int group = (blockIdx.x * blockDim.x + tid) >> a.log2_lanes;
+  const int group = (blockIdx.x * blockDim.x + tid) >> (WARP ? 5 : a.log2_lanes);
   const unsigned wl = tid & 31;
-  const unsigned mask = L >= 32 ? 0xffffffffu : (((1u << L) - 1u) << (wl & ~(unsigned)(L - 1)));
+  const unsigned mask = WARP ? 0xffffffffu : L >= 32 ? 0xffffffffu : (((1u << L) - 1u) << (wl & ~(unsigned)(L - 1)));
   if (group >= a.groups) return;  // whole groups exit together
   const uint64_t keep = policy_keep(1.0f), strm = policy_stream();
   const T *B = (const T *)a.B;
@@ -166,11 +169,21 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
       #pragma unroll
       for (int j = 0; j < NV; j++)
         #pragma unroll
-        for (int i = 0; i < V; i++) {
-          part[u] = fmaf(g[u][j][i], bcur[j][i], part[u]);
-          if (kahan) kahan_fma(acc[j][i], comp[j][i], av[u], g[u][j][i]);
-          else acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
-        }
+        for (int i = 0; i < V; i++) part[u] = fmaf(g[u][j][i], bcur[j][i], part[u]);
+      // one branch per nonzero on the row's (group-uniform) mode; the empty
+      // asm keeps the compiler from computing both steps and selecting
+      if (kahan) {
+        asm volatile("");
+        #pragma unroll
+        for (int j = 0; j < NV; j++)
+          #pragma unroll
+          for (int i = 0; i < V; i++) kahan_fma(acc[j][i], comp[j][i], av[u], g[u][j][i]);
+      } else {
+        #pragma unroll
+        for (int j = 0; j < NV; j++)
+          #pragma unroll
+          for (int i = 0; i < V; i++) acc[j][i] = fmaf(av[u], g[u][j][i], acc[j][i]);
+      }
     }
     // the four dot products: reduced across the lanes, stored at A's positions
     if (L >= BWD_U) {
@@ -192,18 +205,23 @@ __global__ void __launch_bounds__(256) fused_bwd_kernel(BwdArgs a) {
   while (k < r_hi) next_row();
 }
 
-template <typename T, typename TC>
-static void *bwd_ptr(int V, int NV) {
+template <typename T, typename TC, bool WARP>
+static void *bwd_ptr_w(int V, int NV) {
   if (NV == 1) {
-    if (V == 1) return (void *)fused_bwd_kernel<T, TC, 1, 1>;
-    if (V == 2) return (void *)fused_bwd_kernel<T, TC, 2, 1>;
-    if (V == 4) return (void *)fused_bwd_kernel<T, TC, 4, 1>;
+    if (V == 1) return (void *)fused_bwd_kernel<T, TC, 1, 1, WARP>;
+    if (V == 2) return (void *)fused_bwd_kernel<T, TC, 2, 1, WARP>;
+    if (V == 4) return (void *)fused_bwd_kernel<T, TC, 4, 1, WARP>;
   } else {
-    if (V == 1) return (void *)fused_bwd_kernel<T, TC, 1, 2>;
-    if (V == 2) return (void *)fused_bwd_kernel<T, TC, 2, 2>;
-    if (V == 4) return (void *)fused_bwd_kernel<T, TC, 4, 2>;
+    if (V == 1) return (void *)fused_bwd_kernel<T, TC, 1, 2, WARP>;
+    if (V == 2) return (void *)fused_bwd_kernel<T, TC, 2, 2, WARP>;
+    if (V == 4) return (void *)fused_bwd_kernel<T, TC, 4, 2, WARP>;
   }
   return nullptr;
+}
+
+template <typename T, typename TC>
+static void *bwd_ptr(int V, int NV, int lanes) {
+  return lanes == 32 ? bwd_ptr_w<T, TC, true>(V, NV) : bwd_ptr_w<T, TC, false>(V, NV);
 }
 
 }  // namespace ss
@@ -236,10 +254,10 @@ extern "C" ss_status ss_spmm_backward(const ss_csr *AT, const int32_t *perm, con
       ((uintptr_t)values % es) || ((uintptr_t)perm % 4))
     return fail(SS_ERR_ALIGNMENT, "dC / B / dB not aligned to the %d-element vector access", V);
   void *fn = nullptr;
-  if (dt == SS_F32) fn = bwd_ptr<float, float>(V, NV);
-  else if (dt == SS_BF16) fn = dB_dtype == SS_F32 ? bwd_ptr<__nv_bfloat16, float>(V, NV)
-                                                  : bwd_ptr<__nv_bfloat16, __nv_bfloat16>(V, NV);
-  else fn = dB_dtype == SS_F32 ? bwd_ptr<__half, float>(V, NV) : bwd_ptr<__half, __half>(V, NV);
+  if (dt == SS_F32) fn = bwd_ptr<float, float>(V, NV, lanes);
+  else if (dt == SS_BF16) fn = dB_dtype == SS_F32 ? bwd_ptr<__nv_bfloat16, float>(V, NV, lanes)
+                                                  : bwd_ptr<__nv_bfloat16, __nv_bfloat16>(V, NV, lanes);
+  else fn = dB_dtype == SS_F32 ? bwd_ptr<__half, float>(V, NV, lanes) : bwd_ptr<__half, __half>(V, NV, lanes);
   if (!fn) return fail(SS_ERR_UNSUPPORTED_KNOBS, "no fused backward kernel for V=%d NV=%d", V, NV);
   BwdArgs a;
   a.K = K; a.M = M; a.N = N; a.nnz = nnz;
