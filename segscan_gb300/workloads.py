@@ -9,7 +9,8 @@ reproduced on the synthetic matrices the benchmark configurations name.
 
 Cases: spmm-<strategy>-n<N> (strategy ebpr|rbpr|ebsr|rbsr, power-law
 1e6 x 1e6), spmm-ebsr-banded-n64, spmm-ebsr-bf16-n64, segment-<sr|pr>-<sum|max|mean>-n<N>
-(segments = the power-law matrix's rows), transpose, sddmm-n64, batched-bf16-n64,
+(segments = the power-law matrix's rows), transpose, sddmm-n64,
+backward-<f32|bf16>-n<N> (the fused backward of the 2e6 power-law layer), batched-bf16-n64,
 batched-plain-n64 (the same 512 matrices, one launch each).
 --scale shrinks the matrices (rows / scale) for small profiling runs.
 """
@@ -88,6 +89,23 @@ def run(case: str, iters: int, scale: int, knobs: dict | None = None) -> dict:
         Ad = api.CsrMatrix.from_host(A, dev)
         ms = _time(lambda: api.transpose(Ad), iters)
         nb = A.nnz * 4 * 6 + (A.ncol + 1) * 4 * 3  # read cols, write/sort perm, rows, gather values
+    elif parts[0] == "backward":
+        # fused backward (dA.values and dB = A^T dC in one walk over A^T) of
+        # the 2e6 x 2e6 power-law layer (Zipf 2.1 clipped to 50000, seed 4);
+        # backward-<f32|bf16>-n<N>
+        dtype = torch.bfloat16 if parts[1] == "bf16" else torch.float32
+        N = int(parts[2][1:])
+        M = max(1000, 2_000_000 // scale)
+        A = synth.powerlaw(M, M, 2.1, 1, max(10, 50_000 // scale), seed=4)
+        Ad = api.CsrMatrix.from_host(A, dev, dtype)
+        AT, perm = api.transpose(Ad)
+        dC = torch.randn((A.nrow, N), device=dev)
+        Bd = torch.rand((A.ncol, N), device=dev).to(dtype)
+        out16 = dtype if dtype != torch.float32 else None
+        ms = _time(lambda: api.spmm_backward(AT, perm, Ad.values, dC, Bd, out16), iters)
+        vb = 2 if dtype != torch.float32 else 4
+        # A^T's pattern and perm, the values, dC rows once, B and dB once, dvals
+        nb = A.nnz * (4 + 4 + vb + 4) + (A.ncol + 1) * 4 + A.nrow * N * 4 + 2 * A.ncol * N * vb
     elif parts[0] == "sddmm":
         N = int(parts[1][1:])
         A = _powerlaw(scale)
