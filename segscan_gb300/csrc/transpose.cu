@@ -337,7 +337,14 @@ constexpr int TB_T = 1024;            // threads per block (count, scan)
 constexpr int TB_PT = 1024;           // threads per block (partition)
 constexpr int TB_PER = 8;             // nonzeros per thread in a partition tile
 constexpr int TB_E = TB_PT * TB_PER;  // nonzeros per partition tile
-constexpr int TB_ST = 1024;           // threads per block (bucket sort; one block per SM)
+#ifndef SS_TB_ST
+#define SS_TB_ST 1024
+#endif
+#ifndef SS_TB_SORT_BLOCKS
+#define SS_TB_SORT_BLOCKS 1
+#endif
+constexpr int TB_ST = SS_TB_ST;                  // threads per block (bucket sort)
+constexpr int TB_SORT_BLOCKS = SS_TB_SORT_BLOCKS;  // bucket-sort blocks resident per SM
 constexpr int TB_F_LOG2_MAX = 13;  // at most 8192 columns per bucket
 constexpr int TB_NB_MAX = 8192;    // buckets
 #ifndef SS_TB_SORT_SMEM_KB
@@ -409,7 +416,9 @@ static size_t bucket_ws_bytes(const BucketPlan &p, int nnz, BucketWs *w, void *b
 // segment and scans it 32 consecutive entries at a time with shuffles (no
 // shared-memory bank conflicts), then the warps' totals are scanned and
 // applied.  Returns the sum / the maximum to every thread.  wbuf: 33 ints of
-// shared memory.
+// shared memory.  Callers synchronise the block before the call: the scan
+// writes x[] from its first step, and a warp's segment is not the range its
+// own threads filled or read.
 template <bool MAX>
 __device__ int block_scan(int32_t *x, int n, int32_t *wbuf) {
   constexpr int ID = MAX ? INT_MIN : 0;
@@ -597,6 +606,9 @@ __global__ void __launch_bounds__(TB_PT, 1) bucket_partition_kernel(PartArgs a) 
       const int h = lst[i];
       base[i] = h ? atomicAdd(a.cursor + i, h) : 0;
     }
+    // every count is read before the scan overwrites them: with more buckets
+    // than threads a thread reads counts that another warp scans
+    __syncthreads();
     const int valid = block_scan<false>(lst, a.NB, wbuf);  // lst: each bucket's start in the tile
     for (int i = tid; i < a.NB; i += TB_PT) cur[i] = lst[i];
     if (tid == 0) lst[a.NB] = valid;
@@ -687,7 +699,7 @@ __device__ __forceinline__ int stage_bucket(const SortArgs &a, int b, int32_t *r
 // columns are counted, its records placed by column and sorted inside each
 // column, all in shared memory.  A larger bucket is placed and sorted in
 // the output arrays.
-__global__ void __launch_bounds__(TB_ST, 1) bucket_sort_kernel(SortArgs a) {
+__global__ void __launch_bounds__(TB_ST, TB_SORT_BLOCKS) bucket_sort_kernel(SortArgs a) {
   extern __shared__ __align__(16) int32_t sm[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm);  // [4 ints]
   const int stg = a.cap + 8;          // staged array length (alignment slack; a multiple of 4)
@@ -884,7 +896,7 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   sa.t_vals = t_vals;
   sa.vsize = dtype_size(A->value_dtype);
   sa.err = walk_error_ptr();
-  bucket_sort_kernel<<<std::min(pl.NB, sms), TB_ST, sort_smem, s>>>(sa);
+  bucket_sort_kernel<<<std::min(pl.NB, sms * TB_SORT_BLOCKS), TB_ST, sort_smem, s>>>(sa);
   e = cudaGetLastError();
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "transpose launch");
 }

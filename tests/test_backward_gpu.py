@@ -45,10 +45,18 @@ def long_column_matrix():
     return synth._build(M, K, np.concatenate(rows), np.concatenate(cols), rng)
 
 
-@pytest.mark.parametrize("which", ["powerlaw", "long_columns"])
+@pytest.mark.parametrize("which", ["powerlaw", "long_columns", "many_buckets"])
 def test_transpose_matches_oracle(cuda, which):
+    """many_buckets: 1.1 M columns with about five nonzeros each go to more
+    column buckets (1075) than a partition block has threads (1024), so
+    each thread reserves ranges for two buckets."""
     from segscan_gb300 import api
-    csr = powerlaw_medium() if which == "powerlaw" else long_column_matrix()
+    if which == "powerlaw":
+        csr = powerlaw_medium()
+    elif which == "long_columns":
+        csr = long_column_matrix()
+    else:
+        csr = synth.poisson(1_100_000, 1_100_000, 5.0, seed=12)
     A = dev_csr(csr)
     AT, perm = api.transpose(A)
     AT2, perm2 = api.transpose(A)

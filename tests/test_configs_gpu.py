@@ -11,7 +11,10 @@ Configurations (seeded synthetic matrices with the stated distributions):
      +-500 of the diagonal, seed 1, N = 64; segment_coo sum / max / mean over
      both matrices' sorted row ids;
   3. both matrices with values and B stored in BF16 and FP16, FP32
-     accumulation, N in {64, 128}, B seed 2.
+     accumulation, N in {64, 128}, B seed 2;
+  5. the differentiated layer: power law 2e6 x 2e6, Zipf 2.1 clipped to
+     [1, 50000], seed 4, N = 128: the device transpose bit-exact, the fused
+     backward's dB = A^T dC and dA.values against FP64.
 
 Bars: FP32 |C - C64| <= 1e-5 * sum|a*b| per element and 1e-5 normwise;
 segment max bit-exact; 16-bit storage 2e-2 normwise against FP64 on the FP32
@@ -150,3 +153,29 @@ def test_config3_precision(cuda, name, dtype, N):
     B = synth.dense(csr.ncol, N, seed=2)
     C64, _ = oracle(csr, B)
     run_all(csr, B, C64, None, f"{name} {dtype} N={N}", dtype=dtype, normwise=2e-2)
+
+
+def test_config5_transpose_and_backward(cuda):
+    """Config 5 at its size.  The transpose sorts into 1954 column buckets,
+    more than the 1024 threads of a partition block; the fused backward
+    walks the result."""
+    from segscan_gb300 import api
+    csr = synth.powerlaw(2_000_000, 2_000_000, 2.1, 1, 50_000, seed=4)
+    A = dev_csr(csr)
+    AT, perm = api.transpose(A)
+    torch.cuda.synchronize()
+    t_indptr, t_indices, operm = oracle_lib.csr_transpose(csr.indptr, csr.indices, csr.ncol)
+    assert np.array_equal(AT.indptr.cpu().numpy(), t_indptr)
+    assert np.array_equal(AT.indices.cpu().numpy(), t_indices)
+    assert np.array_equal(perm.cpu().numpy(), operm)
+    assert np.array_equal(AT.values.cpu().numpy(), csr.values[operm])
+    N = 128
+    dC = np.random.default_rng(4).standard_normal((csr.nrow, N), dtype=np.float32)
+    B = synth.dense(csr.ncol, N, seed=44)
+    dvals, dB = api.spmm_backward(AT, perm, A.values, torch.from_numpy(dC).cuda(), torch.from_numpy(B).cuda())
+    torch.cuda.synchronize()
+    dB64, absdB = oracle_lib.spmm_f64(t_indptr, t_indices, csr.values[operm], dC, threads=THREADS)
+    check_close(dB.cpu().numpy(), dB64, absdB, 1e-5, 1e-5, "config 5 dB = A^T dC")
+    del dB64, absdB
+    dv64, dvabs = oracle_lib.sddmm_f64(csr.indptr, csr.indices, dC, B)
+    check_close(dvals.cpu().numpy(), dv64, dvabs, 1e-5, 1e-5, "config 5 dA.values")
