@@ -69,9 +69,11 @@ def test_transpose_matches_oracle(cuda, which):
     assert np.array_equal(AT.values.cpu().numpy(), csr.values[operm])
 
 
-@pytest.mark.parametrize("N", [1, 3, 8, 64, 128])
+@pytest.mark.parametrize("N", [1, 3, 8, 64, 128, 160, 256])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
 def test_sddmm(cuda, N, dtype):
+    """N of 128 and more take the whole-warp kernel; 160 and 256 walk two
+    column slices (160: the second one partly idle)."""
     from segscan_gb300 import api
     csr = powerlaw_medium(M=20000, lmax=3000)
     rng = np.random.default_rng(N)
