@@ -650,6 +650,38 @@ __device__ __forceinline__ void insertion_sort2(int32_t *k, int32_t *v, int n) {
   }
 }
 
+// Sorts n <= 8 keys ascending in registers by a fixed network of 19
+// compare-exchanges (Batcher's odd-even merge sort for eight inputs), the
+// entries past n padded with INT_MAX.  The values are sorted by the same
+// network on their own: a column's rows grow with its positions, so the
+// sorted rows are the rows of the sorted positions.  All eight loads are
+// independent, so a column costs one shared-memory round trip instead of a
+// chain of them.
+__device__ __forceinline__ void sort8(int32_t *k, int32_t *v, int n) {
+  int32_t a[8], b[8];
+  #pragma unroll
+  for (int j = 0; j < 8; j++) {
+    a[j] = j < n ? k[j] : INT_MAX;
+    b[j] = j < n ? v[j] : INT_MAX;
+  }
+  constexpr int NET[19][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3}, {4, 6}, {5, 7}, {1, 2}, {5, 6},
+                              {0, 4}, {1, 5}, {2, 6}, {3, 7}, {2, 4}, {3, 5}, {1, 2}, {3, 4}, {5, 6}};
+  #pragma unroll
+  for (int c = 0; c < 19; c++) {
+    const int x = NET[c][0], y = NET[c][1];
+    const int32_t alo = min(a[x], a[y]), ahi = max(a[x], a[y]);
+    const int32_t blo = min(b[x], b[y]), bhi = max(b[x], b[y]);
+    a[x] = alo; a[y] = ahi;
+    b[x] = blo; b[y] = bhi;
+  }
+  #pragma unroll
+  for (int j = 0; j < 8; j++)
+    if (j < n) {
+      k[j] = a[j];
+      v[j] = b[j];
+    }
+}
+
 // Block sort of n keys in global memory: staged through shared memory when
 // they fit.
 __device__ void sort_segment(int32_t *seg, int n, int32_t *stage, int cap) {
@@ -675,6 +707,41 @@ struct SortArgs {
 };
 
 constexpr uint32_t TB_SPIN_LIMIT = 1u << 22;  // mbarrier polls before giving up
+
+// Sorts each of a bucket's columns (cnt: column starts, cnt[nf] the end)
+// shorter than 33 entries by position, one thread per column, the rows
+// moved along; longer columns are listed in longs (count at *nlong) for the
+// block to sort.  kp / vp are shared or global; the call site fixes which.
+__device__ __forceinline__ void sort_short_columns(int32_t *kp, int32_t *vp, const int32_t *cnt, int32_t *longs,
+                                                   int32_t *nlong, int nf) {
+  for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+    const int s = cnt[i], len = cnt[i + 1] - s;
+    if (len > 32) longs[atomicAdd(nlong, 1)] = i;
+    else if (len > 8) insertion_sort2(kp + s, vp + s, len);
+    else if (len > 1) sort8(kp + s, vp + s, len);
+  }
+}
+
+// t_vals[s0 + i] = vals[src[i]] for the bucket's n entries, eight gathers
+// in flight per thread; src is shared or global, the call site fixes which.
+__device__ __forceinline__ void gather_bucket_values(const SortArgs &a, const int32_t *src, int s0, int n) {
+  for (int i0 = 0; i0 < n; i0 += 8 * blockDim.x) {
+    uint32_t v[8];
+    #pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int i = i0 + threadIdx.x + u * blockDim.x;
+      const int p = i < n ? src[i] : 0;
+      v[u] = a.vsize == 4 ? __ldg((const uint32_t *)a.vals + p) : __ldg((const unsigned short *)a.vals + p);
+    }
+    #pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int i = i0 + threadIdx.x + u * blockDim.x;
+      if (i >= n) break;
+      if (a.vsize == 4) ((uint32_t *)a.t_vals)[s0 + i] = v[u];
+      else ((uint16_t *)a.t_vals)[s0 + i] = (uint16_t)v[u];
+    }
+  }
+}
 
 // The records of bucket b into the staging arrays: one bulk copy per array
 // from the 16-byte word holding its first record to the one holding its
@@ -754,6 +821,7 @@ __global__ void __launch_bounds__(TB_ST, TB_SORT_BLOCKS) bucket_sort_kernel(Sort
     }
     // count the bucket's columns
     if (fits) {
+      #pragma unroll 4
       for (int i = tid; i < n; i += TB_ST) {
         const int c = rc[d + i] - c0;
         if ((unsigned)c < (unsigned)nf) atomicAdd(cnt + c, 1);
@@ -779,15 +847,17 @@ __global__ void __launch_bounds__(TB_ST, TB_SORT_BLOCKS) bucket_sort_kernel(Sort
     }
     if (tid == 0) cnt[nf] = total;
     __syncthreads();
-    int32_t *dp = fits ? sp : a.perm + s0;
-    int32_t *dr = fits ? sr : a.t_indices + s0;
+    // The shared-memory and the global-memory paths are written apart, so
+    // every access has a known address space: through a pointer that may be
+    // either, shared accesses become generic ones that queue with the global
+    // loads and stores.
     if (fits) {
       for (int i = tid; i < n; i += TB_ST) {
         const int c = rc[d + i] - c0;
         if ((unsigned)c < (unsigned)nf) {
           const int q = atomicAdd(cur + c, 1);
-          dp[q] = rp[d + i];
-          dr[q] = rr[d + i];
+          sp[q] = rp[d + i];
+          sr[q] = rr[d + i];
         }
       }
       __syncthreads();
@@ -807,8 +877,8 @@ __global__ void __launch_bounds__(TB_ST, TB_SORT_BLOCKS) bucket_sort_kernel(Sort
         for (int u = 0; u < 4; u++) {
           if ((unsigned)c[u] < (unsigned)nf) {
             const int q = atomicAdd(cur + c[u], 1);
-            dp[q] = p[u];
-            dr[q] = r[u];
+            a.perm[s0 + q] = p[u];
+            a.t_indices[s0 + q] = r[u];
           }
         }
       }
@@ -817,11 +887,8 @@ __global__ void __launch_bounds__(TB_ST, TB_SORT_BLOCKS) bucket_sort_kernel(Sort
       if (tid == 0 && fits_at(b + gridDim.x)) wbuf[48] = stage_bucket(a, b + gridDim.x, rc, rp, rr, bar);
     }
     // each column by position: short ones by a thread, long ones by the block
-    for (int i = tid; i < nf; i += TB_ST) {
-      const int s = cnt[i], len = cnt[i + 1] - s;
-      if (len > 32) cur[atomicAdd(wbuf + TB_LONG, 1)] = i;
-      else if (len > 1) insertion_sort2(dp + s, dr + s, len);
-    }
+    if (fits) sort_short_columns(sp, sr, cnt, cur, wbuf + TB_LONG, nf);
+    else sort_short_columns(a.perm + s0, a.t_indices + s0, cnt, cur, wbuf + TB_LONG, nf);
     __syncthreads();
     const int nl = wbuf[TB_LONG];
     for (int l = 0; l < nl; l++) {
@@ -831,8 +898,8 @@ __global__ void __launch_bounds__(TB_ST, TB_SORT_BLOCKS) bucket_sort_kernel(Sort
         bitonic_block(sp + s, len);
         bitonic_block(sr + s, len);
       } else {
-        sort_segment(dp + s, len, sp, 2 * a.cap);
-        sort_segment(dr + s, len, sp, 2 * a.cap);
+        sort_segment(a.perm + s0 + s, len, sp, 2 * a.cap);
+        sort_segment(a.t_indices + s0 + s, len, sp, 2 * a.cap);
       }
     }
     if (fits) {
@@ -842,23 +909,8 @@ __global__ void __launch_bounds__(TB_ST, TB_SORT_BLOCKS) bucket_sort_kernel(Sort
       }
     }
     if (a.t_vals) {  // the values, eight gathers in flight per thread
-      const int32_t *src = fits ? sp : a.perm + s0;
-      for (int i0 = 0; i0 < n; i0 += 8 * TB_ST) {
-        uint32_t v[8];
-        #pragma unroll
-        for (int u = 0; u < 8; u++) {
-          const int i = i0 + tid + u * TB_ST;
-          const int p = i < n ? src[i] : 0;
-          v[u] = a.vsize == 4 ? __ldg((const uint32_t *)a.vals + p) : __ldg((const unsigned short *)a.vals + p);
-        }
-        #pragma unroll
-        for (int u = 0; u < 8; u++) {
-          const int i = i0 + tid + u * TB_ST;
-          if (i >= n) break;
-          if (a.vsize == 4) ((uint32_t *)a.t_vals)[s0 + i] = v[u];
-          else ((uint16_t *)a.t_vals)[s0 + i] = (uint16_t)v[u];
-        }
-      }
+      if (fits) gather_bucket_values(a, sp, s0, n);
+      else gather_bucket_values(a, a.perm + s0, s0, n);
     }
     __syncthreads();  // the next bucket reuses the shared memory
   }
