@@ -189,7 +189,13 @@ __global__ void __launch_bounds__(256, NV == 1 ? 4 : 1) fused_bwd_kernel(BwdArgs
     if (L >= BWD_U) {
       int base = 0;
       const float x = butterfly_sum<BWD_U>(part, lane, L, mask, base);
-      if ((lane & (L / BWD_U - 1)) == 0 && pos[base] >= 0 && pos[base] < a.nnz) a.dvals[pos[base]] = x;
+      // the storing lane reads perm[q0 + base] again (just loaded, cached)
+      // rather than indexing pos[] by a lane-dependent base, which would put
+      // pos in local memory
+      if ((lane & (L / BWD_U - 1)) == 0 && q0 + base < qe) {
+        const int pb = __ldg(a.perm + q0 + base);
+        if ((unsigned)pb < (unsigned)a.nnz) a.dvals[pb] = x;
+      }
     } else {
       #pragma unroll
       for (int u = 0; u < BWD_U; u++) {
