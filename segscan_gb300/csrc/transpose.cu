@@ -334,8 +334,18 @@ static ss_status counting_sort(const int32_t *keys, int nnz, int K, int32_t *out
 // Two-level bucket transpose (ss_csr_transpose)
 // ---------------------------------------------------------------------
 constexpr int TB_T = 1024;            // threads per block (count, scan)
-constexpr int TB_PT = 1024;           // threads per block (partition)
-constexpr int TB_PER = 8;             // nonzeros per thread in a partition tile
+#ifndef SS_TB_PT
+#define SS_TB_PT 1024
+#endif
+#ifndef SS_TB_PER
+#define SS_TB_PER 8
+#endif
+#ifndef SS_TB_PART_BLOCKS
+#define SS_TB_PART_BLOCKS 1
+#endif
+constexpr int TB_PT = SS_TB_PT;                    // threads per block (partition)
+constexpr int TB_PER = SS_TB_PER;                  // nonzeros per thread in a partition tile
+constexpr int TB_PART_BLOCKS = SS_TB_PART_BLOCKS;  // partition blocks resident per SM
 constexpr int TB_E = TB_PT * TB_PER;  // nonzeros per partition tile
 #ifndef SS_TB_ST
 #define SS_TB_ST 1024
@@ -541,7 +551,7 @@ struct PartArgs {
 // (a counting sort of the tile) and written out as one contiguous run per
 // bucket into the range the tile reserved there, so that consecutive
 // threads store consecutive addresses.
-__global__ void __launch_bounds__(TB_PT, 1) bucket_partition_kernel(PartArgs a) {
+__global__ void __launch_bounds__(TB_PT, TB_PART_BLOCKS) bucket_partition_kernel(PartArgs a) {
   extern __shared__ int32_t sm[];
   int32_t *lst = sm;               // [NB + 1]: the tile's count per bucket, then its start in the tile
   int32_t *cur = lst + a.NB + 1;   // [NB]: placement cursors
@@ -939,7 +949,7 @@ static ss_status bucket_transpose(const ss_csr *A, const BucketPlan &pl, int32_t
   pa.indptr = A->indptr; pa.cols = A->indices;
   pa.M = M; pa.K = K; pa.nnz = nnz; pa.f = pl.f; pa.NB = pl.NB;
   pa.cursor = w.cursor; pa.pos = w.pos; pa.row = w.row; pa.col = w.col;
-  bucket_partition_kernel<<<(int)std::min<long long>(tiles, sms), TB_PT, part_smem, s>>>(pa);
+  bucket_partition_kernel<<<(int)std::min<long long>(tiles, (long long)sms * TB_PART_BLOCKS), TB_PT, part_smem, s>>>(pa);
   SortArgs sa;
   sa.start = w.start; sa.pos = w.pos; sa.row = w.row; sa.col = w.col;
   sa.K = K; sa.NB = pl.NB; sa.f = pl.f; sa.F = pl.F; sa.cap = pl.cap;
