@@ -100,6 +100,8 @@ int *walk_error_ptr();
 // streaming multiprocessors of the current device, looked up once per device
 // (util.cu); 1 when the query fails
 int sm_count();
+// L2 size of the current device in bytes (cached per device).
+long long l2_bytes();
 
 // Launchers (kernels live in spmm_rb.cu, eb_walk.cu, eb_scan.cu).
 ss_status launch_rbsr(const SpmmCall &c, const RbGeom &g, cudaStream_t s);

@@ -16,6 +16,8 @@
 //    column indices were loaded during the previous step, dC and B slices
 //    loaded together with 16-bit B kept packed until every load of the step
 //    is issued, compile-time lane masks.
+// B rows are gathered with an evict-last L2 policy; dC rows too when dC fits
+// in half the L2, else evict-first (they are read once, row after row).
 #include "common.cuh"
 #include "eb_common.cuh"
 #include "internal.h"
@@ -41,7 +43,7 @@ __global__ void __launch_bounds__(256) sddmm_rows_kernel(int M, int K, int N, in
                                                          const int32_t *__restrict__ indptr,
                                                          const int32_t *__restrict__ cols, const float *__restrict__ dC,
                                                          const T *__restrict__ B, float *__restrict__ out, int lanes,
-                                                         int log2_lanes) {
+                                                         int log2_lanes, int dc_stream) {
   const int tid = threadIdx.x;
   const int lane = tid & (lanes - 1);
   const int team = (blockIdx.x * blockDim.x + tid) >> log2_lanes;
@@ -49,6 +51,7 @@ __global__ void __launch_bounds__(256) sddmm_rows_kernel(int M, int K, int N, in
   const unsigned wl = tid & 31;
   const unsigned mask = lanes >= 32 ? 0xffffffffu : (((1u << lanes) - 1u) << (wl & ~(unsigned)(lanes - 1)));
   const uint64_t keep = policy_keep(1.0f), strm = policy_stream();
+  const uint64_t dc_pol = dc_stream ? strm : keep;
   const int nchunks = (nnz + SDDMM_CHUNK - 1) / SDDMM_CHUNK;
   for (int chunk = team; chunk < nchunks; chunk += teams) {
     const int cs = chunk * SDDMM_CHUNK, ce = min(cs + SDDMM_CHUNK, nnz);
@@ -69,7 +72,7 @@ __global__ void __launch_bounds__(256) sddmm_rows_kernel(int M, int K, int N, in
         if ((unsigned)c >= (unsigned)K) continue;
         for (int j0 = lane * V; j0 < N; j0 += lanes * V) {
           float g[V], b[V];
-          load_vec<float, V>(dC + (int64_t)row * N + j0, g, keep);
+          load_vec<float, V>(dC + (int64_t)row * N + j0, g, dc_pol);
           load_vec<T, V>(B + (int64_t)c * N + j0, b, keep);
           #pragma unroll
           for (int i = 0; i < V; i++) part[u] = fmaf(g[i], b[i], part[u]);
@@ -91,7 +94,8 @@ __global__ void __launch_bounds__(256) sddmm_rows_kernel(int M, int K, int N, in
 
 struct SddmmArgs {
   int M, K, N, nnz;
-  int slices;  // column slices of 32 * V elements covering N
+  int slices;     // column slices of 32 * V elements covering N
+  int dc_stream;  // dC rows loaded evict-first (dC larger than half the L2)
   const int32_t *indptr, *cols;
   const float *dC;  // [M x N]
   const void *B;    // [K x N], the values' storage type
@@ -110,6 +114,7 @@ __global__ void __launch_bounds__(256, 4) sddmm_warp_kernel(SddmmArgs a) {
   const int team = (blockIdx.x * blockDim.x + tid) >> 5;
   const int teams = (gridDim.x * blockDim.x) >> 5;
   const uint64_t keep = policy_keep(1.0f), strm = policy_stream();
+  const uint64_t dc_pol = a.dc_stream ? strm : keep;
   const T *__restrict__ B = (const T *)a.B;
   const int nchunks = (a.nnz + SDDMM_CHUNK - 1) / SDDMM_CHUNK;
   for (int chunk = team; chunk < nchunks; chunk += teams) {
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(256, 4) sddmm_warp_kernel(SddmmArgs a) {
           #pragma unroll
           for (int i = 0; i < V; i++) g[u][i] = 0.f;
           if (ok[u] && act) {
-            load_vec<float, V>(a.dC + (int64_t)row[u] * a.N + j0, g[u], keep);
+            load_vec<float, V>(a.dC + (int64_t)row[u] * a.N + j0, g[u], dc_pol);
             load_raw<T, V>(B + (int64_t)col[u] * a.N + j0, braw[u], keep);
           }
         }
@@ -229,19 +234,25 @@ extern "C" ss_status ss_sddmm(const ss_csr *A, int N, const float *dC, const voi
   long long blocks = (teams_needed * lanes + threads - 1) / threads;
   if (blocks > (long long)sm_count() * 16) blocks = (long long)sm_count() * 16;
   if (blocks < 1) blocks = 1;
+  // dC is read row after row, each row's reuse served by L1: when it is
+  // larger than half the L2, its lines are marked evict-first so that they
+  // do not push out the gathered B rows; a smaller dC is kept like B
+  const int dc_stream = (long long)A->nrow * N * 4 > l2_bytes() / 2;
   cudaError_t e;
   if (warp) {
     SddmmArgs a;
     a.M = A->nrow; a.K = A->ncol; a.N = N; a.nnz = nnz;
     a.slices = ceil_div(N, lanes * V);
     a.indptr = A->indptr; a.cols = A->indices; a.dC = dC; a.B = B; a.out = dvals;
+    a.dc_stream = dc_stream;
     void *args[] = {&a};
     e = cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, 0, (cudaStream_t)stream);
   } else {
     int log2_lanes = ilog2(lanes);
     int M = A->nrow, K = A->ncol, Nn = N, nz = nnz;
     const int32_t *ip = A->indptr, *ix = A->indices;
-    void *args[] = {&M, &K, &Nn, &nz, &ip, &ix, &dC, &B, &dvals, &lanes, &log2_lanes};
+    int dcs = dc_stream;
+    void *args[] = {&M, &K, &Nn, &nz, &ip, &ix, &dC, &B, &dvals, &lanes, &log2_lanes, &dcs};
     e = cudaLaunchKernel(fn, dim3((unsigned)blocks), dim3(threads), args, 0, (cudaStream_t)stream);
   }
   return e == cudaSuccess ? SS_OK : cuda_fail(e, "sddmm launch");

@@ -27,6 +27,11 @@ int sm_count() {
   return device_attr(cudaDevAttrMultiProcessorCount, cache, 1);
 }
 
+long long l2_bytes() {
+  static std::atomic<int> cache[64];
+  return device_attr(cudaDevAttrL2CacheSize, cache, 64 << 20);
+}
+
 // rows[i] = binary_search_segment_number(indptr, M, nnz, e) for e = elems[i]
 // (test-cg/include/util/check.cuh:88-102), or for e = i when elems is null.
 __global__ void row_ids_kernel(const int32_t *__restrict__ indptr, int M, const int32_t *__restrict__ elems,
