@@ -7,7 +7,7 @@
 // across the lanes by a butterfly.  FP32 math.  Two kernels:
 //  * teams narrower than a warp (N < 32 V): the chunk's first row from one
 //    binary search, later rows followed along indptr (rows only move
-//    forward), eight nonzeros per step; at 31 registers 64 warps per SM
+//    forward), eight nonzeros per step; at 32 registers 64 warps per SM
 //    stay resident;
 //  * whole-warp teams (N >= 32 V): the rows come from a window of indptr
 //    the 32 lanes hold one entry each (the row of position p is the

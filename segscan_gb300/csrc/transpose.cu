@@ -720,8 +720,9 @@ constexpr uint32_t TB_SPIN_LIMIT = 1u << 22;  // mbarrier polls before giving up
 
 // Sorts each of a bucket's columns (cnt: column starts, cnt[nf] the end)
 // shorter than 33 entries by position, one thread per column, the rows
-// moved along; longer columns are listed in longs (count at *nlong) for the
-// block to sort.  kp / vp are shared or global; the call site fixes which.
+// moved along: up to eight entries in registers (sort8), more by insertion.
+// Longer columns are listed in longs (count at *nlong) for the block to
+// sort.  kp / vp are shared or global; the call site fixes which.
 __device__ __forceinline__ void sort_short_columns(int32_t *kp, int32_t *vp, const int32_t *cnt, int32_t *longs,
                                                    int32_t *nlong, int nf) {
   for (int i = threadIdx.x; i < nf; i += blockDim.x) {
