@@ -14,6 +14,14 @@ so the ratio of the two is the traffic the cache capacity forces, and
 algorithmic bytes / (DRAM bytes / rate) is the highest algorithmic fraction
 a kernel can reach at that rate.  CPU only; takes about ten seconds per
 capacity.
+
+With --backward it replays instead the dC row stream of the fused backward
+on the 2e6 x 2e6 layer (Zipf 2.1 clipped to 50000, seed 4): A^T's entries
+(k, i) in A^T order, each reading dC row i, with the kernel's groups
+advancing through their contiguous blocks in lockstep.  Rows of A-rows
+shorter than --hot-min bypass the cache (1: every row is cached):
+
+    python bench_l2_model.py --backward --N 128 --l2-mb 63 126 --hot-min 1 8
 """
 from __future__ import annotations
 
@@ -61,6 +69,41 @@ def model(A: synth.Csr, N: int, l2_mb: list[float], dram_gbs: float, value_bytes
     return out
 
 
+def lru_hits_hot(stream: np.ndarray, lens: np.ndarray, lines: int, hot_min: int) -> int:
+    """Hits of an LRU of `lines` rows that only rows with lens >= hot_min enter."""
+    cache: OrderedDict = OrderedDict()
+    hits = 0
+    for x, n in zip(stream.tolist(), lens.tolist()):
+        if n < hot_min:
+            continue
+        if x in cache:
+            hits += 1
+            cache.move_to_end(x)
+        else:
+            cache[x] = None
+            if len(cache) > lines:
+                cache.popitem(last=False)
+    return hits
+
+
+def backward_model(N: int, l2_mb: list[float], hot_mins: list[int], groups: int) -> dict:
+    A = synth.powerlaw(2_000_000, 2_000_000, 2.1, 1, 50_000, seed=4)
+    rowlen = np.diff(A.indptr)
+    rows = np.repeat(np.arange(A.nrow, dtype=np.int64), rowlen)  # A's row of each nonzero
+    seq = rows[np.argsort(A.indices, kind="stable")]               # the dC row of each A^T entry
+    blk = -(-seq.size // groups)
+    q = np.arange(seq.size)
+    stream = seq[np.lexsort((q // blk, q % blk))]                  # groups in lockstep
+    lens = rowlen[stream]
+    out = {"nnz": int(seq.size), "row_bytes": N * 4, "groups": groups, "capacities": []}
+    for mb in l2_mb:
+        lines = int(mb * 2 ** 20 / (N * 4))
+        for h in hot_mins:
+            hits = lru_hits_hot(stream, lens, lines, h)
+            out["capacities"].append({"l2_mb": mb, "hot_min": h, "hit_rate": round(hits / seq.size, 4)})
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--N", type=int, default=64)
@@ -68,7 +111,14 @@ def main(argv=None):
     ap.add_argument("--dram-gbs", type=float, default=5100.0,
                     help="DRAM rate of random row reads mixed with C writes")
     ap.add_argument("--peak-gbs", type=float, default=None, help="adds alg_gbs_ceiling / peak")
+    ap.add_argument("--backward", action="store_true", help="the fused backward's dC stream instead")
+    ap.add_argument("--hot-min", type=int, nargs="+", default=[1])
+    ap.add_argument("--groups", type=int, default=152 * 4 * 8 * 2,
+                    help="backward: groups walking A^T (about the resident ones)")
     a = ap.parse_args(argv)
+    if a.backward:
+        print(json.dumps(backward_model(a.N, a.l2_mb, a.hot_min, a.groups), indent=1))
+        return
     A = synth.powerlaw(1_000_000, 1_000_000, 2.1, 1, 20000, seed=1)
     out = model(A, a.N, a.l2_mb, a.dram_gbs)
     if a.peak_gbs:
